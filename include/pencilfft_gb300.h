@@ -1,0 +1,173 @@
+/*
+ * pencilfft_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * PencilFFTs.jl transform path (one GPU, proc_dims all ones, no MPI).
+ *
+ * All entry points are plain C: integers, sizes and untyped pointers.  Device
+ * buffers are raw CUDA device pointers owned by the caller; `stream` is a
+ * cudaStream_t passed as `void*` (NULL = legacy default stream).  Every
+ * function returns PFGB_OK (0) or a negative status; the message of the last
+ * failure on the calling thread is available from pfgb_last_error().
+ *
+ * Array conventions follow the reference (column-major, Julia indexing):
+ *   - input arrays are stored in natural memory order, dimension 1 fastest,
+ *     extra (untransformed) dimensions slowest;
+ *   - output arrays are stored with the transformed dimensions in reversed
+ *     memory order (dimension N fastest) when permute_dims != 0, otherwise in
+ *     natural order (reference src/plans.jl:503-521);
+ *   - in-place real-to-complex plans (RFFT!) use one buffer whose real view is
+ *     padded to 2*(n1/2+1) reals along dimension 1 (reference
+ *     src/multiarrays_r2c.jl:69-79).
+ */
+#ifndef PENCILFFT_GB300_H
+#define PENCILFFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFGB_MAX_DIMS 8  /* transformed dimensions */
+#define PFGB_MAX_EXTRA 4 /* extra (untransformed, batch) dimensions */
+
+/* Status codes.  The ArgumentError cases of the reference map to
+ * PFGB_ERR_ARGUMENT. */
+enum {
+  PFGB_OK = 0,
+  PFGB_ERR_ARGUMENT = -1,    /* invalid descriptor / arrays (ArgumentError) */
+  PFGB_ERR_UNSUPPORTED = -2, /* valid request that this build cannot run */
+  PFGB_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+  PFGB_ERR_ALLOC = -4        /* device or host allocation failed */
+};
+
+/* Transform kinds: one per dimension (reference src/Transforms/*.jl). */
+enum {
+  PFGB_FFT = 0,         /* Transforms.FFT / FFT!   (c2c, sign -1) */
+  PFGB_BFFT = 1,        /* Transforms.BFFT / BFFT! (c2c, sign +1, unnormalised) */
+  PFGB_RFFT = 2,        /* Transforms.RFFT / RFFT! (r2c, n -> n/2+1) */
+  PFGB_BRFFT = 3,       /* Transforms.BRFFT(d) / BRFFT!(d) (c2r); see brfft_even */
+  PFGB_R2R = 4,         /* Transforms.R2R(kind) / R2R!(kind); see r2r_kind */
+  PFGB_NOTRANSFORM = 5  /* Transforms.NoTransform / NoTransform! */
+};
+
+/* FFTW's r2r kind codes (fftw3.h), accepted unchanged in r2r_kind.  R2HC and
+ * HC2R are rejected, as in the reference (src/Transforms/r2r.jl:42-45). */
+enum {
+  PFGB_R2HC = 0, PFGB_HC2R = 1, PFGB_DHT = 2,
+  PFGB_REDFT00 = 3, PFGB_REDFT01 = 4, PFGB_REDFT10 = 5, PFGB_REDFT11 = 6,
+  PFGB_RODFT00 = 7, PFGB_RODFT01 = 8, PFGB_RODFT10 = 9, PFGB_RODFT11 = 10
+};
+
+/* Plan descriptor: the arguments of
+ *   PencilFFTPlan(dims_global, transforms, proc_dims, comm, real_type;
+ *                 extra_dims, permute_dims)      (reference src/plans.jl:306-320)
+ * with proc_dims all ones.  A single transform expanded over all dimensions
+ * (reference Transforms.expand_dims) is given here already expanded. */
+typedef struct pfgb_plan_desc {
+  int32_t ndims;                      /* N >= 1 */
+  int64_t dims[PFGB_MAX_DIMS];        /* global input sizes (logical order) */
+  int32_t kind[PFGB_MAX_DIMS];        /* PFGB_FFT ... PFGB_NOTRANSFORM */
+  int32_t inplace[PFGB_MAX_DIMS];     /* 1 for the "!" variants */
+  int32_t r2r_kind[PFGB_MAX_DIMS];    /* FFTW kind code when kind == PFGB_R2R */
+  int32_t brfft_even[PFGB_MAX_DIMS];  /* BRFFT.even_output when kind == PFGB_BRFFT */
+  int32_t real_bytes;                 /* 4 (Float32) or 8 (Float64) */
+  int32_t permute_dims;               /* 1 = Val(true) (default), 0 = Val(false) */
+  int32_t n_extra;                    /* number of extra_dims */
+  int64_t extra_dims[PFGB_MAX_EXTRA];
+  int32_t precision_mode;             /* 0 = plain arithmetic of real_bytes */
+  int32_t autotune;                   /* 0 = off */
+} pfgb_plan_desc;
+
+typedef struct pfgb_plan pfgb_plan;
+
+/* Information about a plan (reference: size(plan), size_global of the input
+ * and output pencils, eltype_input/eltype_output, scale_factor, is_inplace). */
+typedef struct pfgb_plan_info {
+  int32_t ndims;
+  int64_t dims_in[PFGB_MAX_DIMS];   /* logical global sizes of the input */
+  int64_t dims_out[PFGB_MAX_DIMS];  /* logical global sizes of the output */
+  int32_t perm_out[PFGB_MAX_DIMS];  /* memory order of the output: perm_out[0]
+                                       is the fastest logical dim (0-based) */
+  int32_t eltype_in_complex;        /* 1 if the input element is complex */
+  int32_t eltype_out_complex;
+  int32_t real_bytes;
+  int32_t inplace;
+  double scale_factor;              /* product of the per-dimension scales */
+  int64_t input_bytes;              /* bytes of the input array (out-of-place) */
+  int64_t output_bytes;             /* bytes of the output array (out-of-place) */
+  int64_t inplace_bytes;            /* bytes of the aliased buffer (in-place) */
+  int64_t scratch_bytes;            /* device scratch the plan holds */
+  int32_t n_passes_forward;         /* kernel passes per forward transform */
+  int32_t n_passes_backward;
+} pfgb_plan_info;
+
+/* Creates a plan (reference PencilFFTPlan constructor, src/plans.jl:241-320,
+ * and the 1D plans of src/plans.jl:523-553).  Allocates the device tables and
+ * scratch on the current CUDA device. */
+int pfgb_plan_create(const pfgb_plan_desc* desc, pfgb_plan** plan);
+
+/* Validates a descriptor and fills `info` as pfgb_plan_create would, on the
+ * host only: no device memory is allocated and no CUDA call is made. */
+int pfgb_plan_query(const pfgb_plan_desc* desc, pfgb_plan_info* info);
+
+/* Releases a plan and its device memory. */
+int pfgb_plan_destroy(pfgb_plan* plan);
+
+/* Fills `info` (reference size(p), scale_factor(p), is_inplace(p),
+ * eltype_input/output(p), pencil_output(p) permutation). */
+int pfgb_plan_info_get(const pfgb_plan* plan, pfgb_plan_info* info);
+
+/* Forward transform: reference LinearAlgebra.mul!(dst, p, src)
+ * (src/operations.jl:24-31).  Out-of-place plans require non-aliased buffers
+ * and leave src unchanged; in-place plans require dst == src. */
+int pfgb_forward(pfgb_plan* plan, void* dst, const void* src, void* stream);
+
+/* Backward transform: reference ldiv!(dst, p, src) when normalise != 0
+ * (src/operations.jl:44-52, scaling fused into the last pass) and
+ * bmul!(dst, p, src) when normalise == 0 (src/operations.jl:34-41). */
+int pfgb_backward(pfgb_plan* plan, void* dst, const void* src, void* stream,
+                  int normalise);
+
+/* Applies one plan to a collection of arrays (reference mul!/ldiv!/bmul!
+ * broadcast over tuples or arrays of PencilArrays, src/operations.jl:129-152).
+ * direction: +1 forward, -1 backward; normalise as in pfgb_backward. */
+int pfgb_execute_many(pfgb_plan* plan, int direction, int normalise,
+                      void* const* dst, const void* const* src, int n,
+                      void* stream);
+
+/* Per-pass timing (replaces the reference's opt-in TimerOutputs sections
+ * "PencilFFTs mul!", "FFT", ..., src/operations.jl:27,37,47,250,288,299).
+ * When enabled, every kernel launch of the plan is bracketed by CUDA events
+ * recorded on the launch stream. */
+typedef struct pfgb_pass_timing {
+  int32_t direction;      /* +1 forward, -1 backward */
+  int32_t pass;           /* index of the pass within its direction */
+  int32_t axis;           /* transformed logical dim (0-based), -1 for copies */
+  int32_t op;             /* internal operation code */
+  int32_t launches;       /* launches recorded since the last reset */
+  double total_ms;        /* summed event time of those launches */
+  int64_t bytes_per_launch; /* algorithmic bytes: one read of the input plus
+                               one write of the output of the pass */
+  char kernel[48];        /* kernel name */
+} pfgb_pass_timing;
+
+/* Enables (on != 0) or disables per-launch event timing and clears the record. */
+int pfgb_plan_set_timing(pfgb_plan* plan, int on);
+
+/* Synchronises on the recorded events and writes up to `max` per-pass entries
+ * into `out`; `*n` receives the number of entries. Clears the record. */
+int pfgb_plan_get_timing(pfgb_plan* plan, pfgb_pass_timing* out, int max, int* n);
+
+/* Copies the message of the last failure on this thread into buf. Returns the
+ * message length. */
+int pfgb_last_error(char* buf, size_t n);
+
+/* Library version string. */
+const char* pfgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PENCILFFT_GB300_H */

@@ -1,0 +1,589 @@
+// Device code of the generic transform pass.
+//
+// One launch performs one 1D transform along one axis of an N-D array (one
+// "pass" of the reference's per-dimension loop, src/operations.jl:227-254),
+// with the pencil re-layout of PencilArrays' transpose! fused into the same
+// pass: a CTA loads a tile of lines into shared memory with coalesced reads
+// in the input layout, transforms every line there (Stockham autosort or
+// Bluestein), and stores the tile with coalesced writes in the output layout.
+//
+// The arithmetic type R is a template parameter (float or double here); the
+// complex element type in memory is Cx<R>.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pfgb {
+
+constexpr int kMaxStages = 8;
+constexpr int kMaxOuter = 12;
+
+// Operation performed by a pass.
+enum PassOp : int {
+  OP_C2C = 0,    // complex -> complex DFT (sign in PassArgs::sign)
+  OP_R2C = 1,    // two real lines packed in one complex DFT, n -> n/2+1
+  OP_C2R = 2,    // two Hermitian half-spectra packed in one complex DFT, m -> n
+  OP_R2R_C = 3,  // real-to-real kind applied to complex data
+  OP_R2R_R = 4,  // real-to-real kind applied to real data (two lines packed)
+};
+
+// FFTW r2r kind codes.
+enum R2RKind : int {
+  K_DHT = 2, K_REDFT00 = 3, K_REDFT01 = 4, K_REDFT10 = 5, K_REDFT11 = 6,
+  K_RODFT00 = 7, K_RODFT01 = 8, K_RODFT10 = 9, K_RODFT11 = 10
+};
+
+// Kernel argument block (host fills it, passed by value).
+struct PassArgs {
+  const void* in;
+  void* out;
+  const void* tw;     // core twiddles: Lc entries exp(-2 pi i m / Lc)
+  const void* chirp;  // Bluestein chirp (M entries) for this pass's sign
+  const void* bfilt;  // Bluestein filter spectrum / L (L entries) for this sign
+  const void* r2rtw;  // r2r twiddles exp(-i pi m / (4 n)), m in [0, 4n]
+  int op, r2r_kind, sign, scale_on;
+  int n_in, n_out;    // line length (elements) in input / output
+  int M;              // DFT length
+  int L;              // Bluestein convolution length (0: direct Stockham of M)
+  int nst;            // number of Stockham stages of the core length
+  int rad[kMaxStages];
+  int lines;          // array lines per tile (input lines)
+  int clines;         // complex lines per tile (lines or lines/2 when packed)
+  int bpl;            // threads per complex line in the core
+  int lp;             // shared-memory pitch of one complex line (elements)
+  int zero_fill;      // clear the tile before the load
+  int in_tfast, out_tfast;  // tile dimension has stride 1 in input / output
+  int nouter;
+  int64_t nt;         // extent of the tile dimension
+  int64_t ntiles;     // ceil(nt / lines)
+  int64_t in_sa, in_st, out_sa, out_st;  // axis and tile strides (elements)
+  int64_t osz[kMaxOuter], in_so[kMaxOuter], out_so[kMaxOuter];
+  double scale;
+};
+
+template <typename R>
+struct Cx {
+  R re, im;
+};
+
+template <typename R>
+__device__ __forceinline__ Cx<R> mk(R a, R b) {
+  Cx<R> z;
+  z.re = a;
+  z.im = b;
+  return z;
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> operator+(Cx<R> a, Cx<R> b) { return mk(a.re + b.re, a.im + b.im); }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a, Cx<R> b) { return mk(a.re - b.re, a.im - b.im); }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a) { return mk(-a.re, -a.im); }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator*(Cx<R> a, Cx<R> b) {
+  return mk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> scal(Cx<R> a, R s) { return mk(a.re * s, a.im * s); }
+template <typename R>
+__device__ __forceinline__ Cx<R> conj(Cx<R> a) { return mk(a.re, -a.im); }
+// multiply by i
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_i(Cx<R> a) { return mk(-a.im, a.re); }
+// multiply by -i
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_mi(Cx<R> a) { return mk(a.im, -a.re); }
+// multiply by the quarter-turn root exp(SIGN * i pi / 2)
+template <int SIGN, typename R>
+__device__ __forceinline__ Cx<R> mul_w4(Cx<R> a) { return SIGN < 0 ? mul_mi(a) : mul_i(a); }
+
+template <typename R>
+__device__ __forceinline__ Cx<R> ldtw(const void* t, int m) {
+  return reinterpret_cast<const Cx<R>*>(t)[m];
+}
+// exp(SIGN * 2 pi i m / Lc) from the table of exp(-2 pi i m / Lc).
+template <int SIGN, typename R>
+__device__ __forceinline__ Cx<R> twid(const void* t, int m) {
+  Cx<R> w = ldtw<R>(t, m);
+  return SIGN < 0 ? w : conj(w);
+}
+
+// ---------------------------------------------------------------------------
+// Small DFT butterflies, y_k = sum_j v_j exp(SIGN 2 pi i jk / RAD), in place.
+// ---------------------------------------------------------------------------
+template <int SIGN, typename R>
+__device__ __forceinline__ void dft2(Cx<R>& a, Cx<R>& b) {
+  Cx<R> t = a;
+  a = t + b;
+  b = t - b;
+}
+
+template <int SIGN, typename R>
+__device__ __forceinline__ void dft4(Cx<R>& x0, Cx<R>& x1, Cx<R>& x2, Cx<R>& x3) {
+  Cx<R> t0 = x0 + x2, t1 = x0 - x2, t2 = x1 + x3, t3 = mul_w4<SIGN>(x1 - x3);
+  x0 = t0 + t2;
+  x2 = t0 - t2;
+  x1 = t1 + t3;
+  x3 = t1 - t3;
+}
+
+// exp(SIGN i pi m / 8) for the compile-time exponent m in [0, 16).
+template <int SIGN, int m, typename R>
+__device__ __forceinline__ Cx<R> w16mul(Cx<R> x) {
+  constexpr int mm = m & 15;
+  const R c1 = R(0.92387953251128675613);  // cos(pi/8)
+  const R s1 = R(0.38268343236508977173);  // sin(pi/8)
+  const R h = R(0.70710678118654752440);   // cos(pi/4)
+  const R sg = SIGN < 0 ? R(-1) : R(1);
+  if (mm == 0) return x;
+  if (mm == 4) return mul_w4<SIGN>(x);
+  if (mm == 8) return -x;
+  if (mm == 12) return mul_w4<-SIGN>(x);
+  // general: angle = SIGN * pi * mm / 8
+  R c, s;
+  switch (mm) {
+    case 1: c = c1; s = s1; break;
+    case 2: c = h; s = h; break;
+    case 3: c = s1; s = c1; break;
+    case 5: c = -s1; s = c1; break;
+    case 6: c = -h; s = h; break;
+    case 7: c = -c1; s = s1; break;
+    case 9: c = -c1; s = -s1; break;
+    case 10: c = -h; s = -h; break;
+    case 11: c = -s1; s = -c1; break;
+    case 13: c = s1; s = -c1; break;
+    case 14: c = h; s = -h; break;
+    default: c = c1; s = -s1; break;  // 15
+  }
+  s = sg * s;
+  return mk(x.re * c - x.im * s, x.re * s + x.im * c);
+}
+
+template <int SIGN, typename R>
+__device__ __forceinline__ void dft8(Cx<R>* v) {
+  // n = n1 + 2 n2, k = k2 + 4 k1
+  dft4<SIGN>(v[0], v[2], v[4], v[6]);
+  dft4<SIGN>(v[1], v[3], v[5], v[7]);
+  v[3] = w16mul<SIGN, 2>(v[3]);
+  v[5] = w16mul<SIGN, 4>(v[5]);
+  v[7] = w16mul<SIGN, 6>(v[7]);
+  // a[n1][k2] sits at v[n1 + 2 k2]
+  Cx<R> y[8];
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) {
+    Cx<R> a0 = v[2 * k2], a1 = v[2 * k2 + 1];
+    y[k2] = a0 + a1;
+    y[k2 + 4] = a0 - a1;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = y[i];
+}
+
+template <int SIGN, typename R>
+__device__ __forceinline__ void dft16(Cx<R>* v) {
+  // n = n1 + 4 n2, k = k2 + 4 k1; a[n1][k2] lives in v[n1 + 4 k2]
+  dft4<SIGN>(v[0], v[4], v[8], v[12]);
+  dft4<SIGN>(v[1], v[5], v[9], v[13]);
+  dft4<SIGN>(v[2], v[6], v[10], v[14]);
+  dft4<SIGN>(v[3], v[7], v[11], v[15]);
+  v[5] = w16mul<SIGN, 1>(v[5]);
+  v[9] = w16mul<SIGN, 2>(v[9]);
+  v[13] = w16mul<SIGN, 3>(v[13]);
+  v[6] = w16mul<SIGN, 2>(v[6]);
+  v[10] = w16mul<SIGN, 4>(v[10]);
+  v[14] = w16mul<SIGN, 6>(v[14]);
+  v[7] = w16mul<SIGN, 3>(v[7]);
+  v[11] = w16mul<SIGN, 6>(v[11]);
+  v[15] = w16mul<SIGN, 9>(v[15]);
+  Cx<R> y[16];
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) {
+    Cx<R> a0 = v[4 * k2], a1 = v[4 * k2 + 1], a2 = v[4 * k2 + 2], a3 = v[4 * k2 + 3];
+    dft4<SIGN>(a0, a1, a2, a3);
+    y[k2] = a0;
+    y[k2 + 4] = a1;
+    y[k2 + 8] = a2;
+    y[k2 + 12] = a3;
+  }
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = y[i];
+}
+
+// Odd prime radix via the symmetric real/imaginary split; the roots of unity
+// come from the core twiddle table (RAD divides the core length Lc).
+template <int RAD, int SIGN, typename R>
+__device__ __forceinline__ void dft_odd(Cx<R>* v, const void* tw, int Lc) {
+  constexpr int H = (RAD - 1) / 2;
+  const int step = Lc / RAD;
+  Cx<R> s[H], d[H];
+  Cx<R> y0 = v[0];
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    s[j - 1] = v[j] + v[RAD - j];
+    d[j - 1] = v[j] - v[RAD - j];
+    y0 = y0 + s[j - 1];
+  }
+  Cx<R> y[RAD];
+  y[0] = y0;
+#pragma unroll
+  for (int k = 1; k <= H; ++k) {
+    Cx<R> a = v[0], b = mk(R(0), R(0));
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+      const int m = (j * k) % RAD;
+      Cx<R> w = ldtw<R>(tw, m * step);  // (cos t, -sin t), t = 2 pi m / RAD
+      a = a + scal(s[j - 1], w.re);
+      b = b + scal(d[j - 1], -w.im);    // sum d_j sin t
+    }
+    // sign -1: y_k = a - i b, y_{RAD-k} = a + i b
+    Cx<R> ib = mul_i(b);
+    if (SIGN < 0) {
+      y[k] = a - ib;
+      y[RAD - k] = a + ib;
+    } else {
+      y[k] = a + ib;
+      y[RAD - k] = a - ib;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < RAD; ++i) v[i] = y[i];
+}
+
+template <int RAD, int SIGN, typename R>
+__device__ __forceinline__ void dft_any(Cx<R>* v, const void* tw, int Lc) {
+  if constexpr (RAD == 2) {
+    dft2<SIGN>(v[0], v[1]);
+  } else if constexpr (RAD == 4) {
+    dft4<SIGN>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (RAD == 8) {
+    dft8<SIGN>(v);
+  } else if constexpr (RAD == 16) {
+    dft16<SIGN>(v);
+  } else {
+    dft_odd<RAD, SIGN>(v, tw, Lc);
+  }
+}
+
+// One Stockham stage of radix RAD on every complex line of the tile.
+// Line length Lc, already-transformed sub-length Ls.  Thread (p, b) does
+// butterfly b of line p: reads z[b + r T], writes z[(b - j) RAD + j + r Ls],
+// j = b mod Ls, T = Lc / RAD.
+template <int RAD, int SIGN, typename R>
+__device__ __forceinline__ void stage(Cx<R>* zl, bool line_ok, int b, int Lc, int Ls,
+                                      const void* tw) {
+  const int T = Lc / RAD;
+  const bool act = line_ok && b < T;
+  Cx<R> v[RAD];
+  int j = 0;
+  if (act) {
+    j = b % Ls;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) v[r] = zl[b + r * T];
+    if (Ls > 1) {
+      const int tstep = j * (Lc / (Ls * RAD));
+#pragma unroll
+      for (int r = 1; r < RAD; ++r) v[r] = v[r] * twid<SIGN, R>(tw, r * tstep);
+    }
+    dft_any<RAD, SIGN>(v, tw, Lc);
+  }
+  __syncthreads();
+  if (act) {
+    const int base = (b - j) * RAD + j;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) zl[base + r * Ls] = v[r];
+  }
+  __syncthreads();
+}
+
+template <int SIGN, typename R>
+__device__ void stockham(Cx<R>* z, const PassArgs& a, int Lc) {
+  const int p = threadIdx.x / a.bpl;
+  const int b = threadIdx.x % a.bpl;
+  const bool line_ok = p < a.clines;
+  Cx<R>* zl = z + (size_t)(line_ok ? p : 0) * a.lp;
+  int Ls = 1;
+  for (int s = 0; s < a.nst; ++s) {
+    const int rd = a.rad[s];
+    switch (rd) {
+      case 2: stage<2, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 3: stage<3, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 4: stage<4, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 5: stage<5, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 7: stage<7, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 8: stage<8, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 11: stage<11, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      case 13: stage<13, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+      default: stage<16, SIGN, R>(zl, line_ok, b, Lc, Ls, a.tw); break;
+    }
+    Ls *= rd;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pre-op: place one complex input value x (array line p of the tile, index j)
+// into the complex DFT line zl (length M).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void r2r_pre(Cx<R>* zl, const PassArgs& a, int j, Cx<R> x) {
+  const int n = a.n_in;
+  const int M = a.M;
+  switch (a.r2r_kind) {
+    case K_DHT:
+      zl[j] = x;
+      break;
+    case K_REDFT00:
+      zl[j] = x;
+      if (j >= 1 && j <= n - 2) zl[M - j] = x;
+      break;
+    case K_RODFT00:
+      zl[j + 1] = x;
+      zl[M - 1 - j] = -x;
+      break;
+    case K_REDFT10:
+      zl[j] = x;
+      zl[2 * n - 1 - j] = x;
+      break;
+    case K_RODFT10:
+      zl[j] = x;
+      zl[2 * n - 1 - j] = -x;
+      break;
+    case K_REDFT11:
+      zl[j] = x * ldtw<R>(a.r2rtw, 2 * j);
+      zl[2 * n - 1 - j] = -(x * ldtw<R>(a.r2rtw, 2 * (2 * n - 1 - j)));
+      break;
+    case K_RODFT11:
+      zl[j] = x * ldtw<R>(a.r2rtw, 2 * j);
+      zl[2 * n - 1 - j] = x * ldtw<R>(a.r2rtw, 2 * (2 * n - 1 - j));
+      break;
+    case K_REDFT01: {
+      Cx<R> y = x * ldtw<R>(a.r2rtw, 2 * j);
+      zl[j] = j == 0 ? scal(y, R(0.5)) : y;
+      break;
+    }
+    default: {  // K_RODFT01
+      Cx<R> y = mul_i(x * ldtw<R>(a.r2rtw, 2 * (j + 1)));
+      zl[j + 1] = j == n - 1 ? scal(y, R(0.5)) : y;
+      break;
+    }
+  }
+}
+
+// R2R post-op: output k of line zl (length M).
+template <typename R>
+__device__ __forceinline__ Cx<R> r2r_post(const Cx<R>* zl, const PassArgs& a, int k) {
+  const int n = a.n_out;
+  const int M = a.M;
+  switch (a.r2r_kind) {
+    case K_DHT: {
+      Cx<R> f = zl[k], g = zl[k == 0 ? 0 : M - k];
+      // ((1+i) f + (1-i) g) / 2
+      Cx<R> s = f + g, d = f - g;
+      return scal(s + mul_i(d), R(0.5));
+    }
+    case K_REDFT00:
+      return zl[k];
+    case K_RODFT00:
+      return mul_i(zl[k + 1]);
+    case K_REDFT10:
+      return ldtw<R>(a.r2rtw, 2 * k) * zl[k];
+    case K_RODFT10:
+      return mul_i(ldtw<R>(a.r2rtw, 2 * (k + 1)) * zl[k + 1]);
+    case K_REDFT11:
+      return ldtw<R>(a.r2rtw, 2 * k + 1) * zl[k];
+    case K_RODFT11:
+      return mul_i(ldtw<R>(a.r2rtw, 2 * k + 1) * zl[k]);
+    case K_REDFT01:
+      return zl[k] + zl[2 * n - 1 - k];
+    default:  // K_RODFT01
+      return zl[k] - zl[2 * n - 1 - k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The pass kernel.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
+  const int nth = blockDim.x;
+  const int tid = threadIdx.x;
+
+  // Tile decode: tile index along the tile dimension, then outer indices.
+  int64_t bid = blockIdx.x;
+  const int64_t tile = bid % a.ntiles;
+  int64_t rest = bid / a.ntiles;
+  const int64_t t0 = tile * a.lines;
+  int64_t ioff = t0 * a.in_st, ooff = t0 * a.out_st;
+  for (int d = 0; d < a.nouter; ++d) {
+    const int64_t idx = rest % a.osz[d];
+    rest /= a.osz[d];
+    ioff += idx * a.in_so[d];
+    ooff += idx * a.out_so[d];
+  }
+  const int nvalid = (int)min((int64_t)a.lines, a.nt - t0);
+  const int Lc = a.L > 0 ? a.L : a.M;
+
+  if (a.zero_fill) {
+    const int tot = a.clines * a.lp;
+    for (int e = tid; e < tot; e += nth) z[e] = mk(R(0), R(0));
+    __syncthreads();
+  }
+
+  // ---- load ----
+  const int op = a.op;
+  if (op == OP_C2C || op == OP_R2R_C) {
+    const Cx<R>* in = reinterpret_cast<const Cx<R>*>(a.in) + ioff;
+    const int tot = a.lines * a.n_in;
+    for (int e = tid; e < tot; e += nth) {
+      int i, j;
+      if (a.in_tfast) { i = e % a.lines; j = e / a.lines; } else { j = e % a.n_in; i = e / a.n_in; }
+      Cx<R> x = mk(R(0), R(0));
+      if (i < nvalid) x = in[(int64_t)j * a.in_sa + (int64_t)i * a.in_st];
+      Cx<R>* zl = z + (size_t)i * a.lp;
+      if (op == OP_C2C) zl[j] = x; else r2r_pre(zl, a, j, x);
+    }
+  } else if (op == OP_R2C || op == OP_R2R_R) {
+    const R* in = reinterpret_cast<const R*>(a.in) + ioff;
+    const int tot = a.clines * a.n_in;
+    for (int e = tid; e < tot; e += nth) {
+      int p, j;
+      if (a.in_tfast) { p = e % a.clines; j = e / a.clines; } else { j = e % a.n_in; p = e / a.n_in; }
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      R xr = R(0), xi = R(0);
+      if (i0 < nvalid) xr = in[(int64_t)j * a.in_sa + (int64_t)i0 * a.in_st];
+      if (i1 < nvalid) xi = in[(int64_t)j * a.in_sa + (int64_t)i1 * a.in_st];
+      Cx<R>* zl = z + (size_t)p * a.lp;
+      if (op == OP_R2C) zl[j] = mk(xr, xi); else r2r_pre(zl, a, j, mk(xr, xi));
+    }
+  } else {  // OP_C2R
+    const Cx<R>* in = reinterpret_cast<const Cx<R>*>(a.in) + ioff;
+    const int n = a.M, m = a.n_in;
+    const int tot = a.clines * m;
+    for (int e = tid; e < tot; e += nth) {
+      int p, k;
+      if (a.in_tfast) { p = e % a.clines; k = e / a.clines; } else { k = e % m; p = e / m; }
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      Cx<R> A = mk(R(0), R(0)), B = mk(R(0), R(0));
+      if (i0 < nvalid) A = in[(int64_t)k * a.in_sa + (int64_t)i0 * a.in_st];
+      if (i1 < nvalid) B = in[(int64_t)k * a.in_sa + (int64_t)i1 * a.in_st];
+      if (k == 0 || 2 * k == n) { A.im = R(0); B.im = R(0); }
+      Cx<R>* zl = z + (size_t)p * a.lp;
+      zl[k] = mk(A.re - B.im, A.im + B.re);                        // A + i B
+      if (k >= 1 && k <= n - m) zl[n - k] = mk(A.re + B.im, B.re - A.im);  // conj(A) + i conj(B)
+    }
+  }
+  __syncthreads();
+
+  // ---- core DFT ----
+  if (a.L == 0) {
+    if (a.sign < 0) stockham<-1, R>(z, a, Lc); else stockham<1, R>(z, a, Lc);
+  } else {
+    const Cx<R>* chirp = reinterpret_cast<const Cx<R>*>(a.chirp);
+    const Cx<R>* bf = reinterpret_cast<const Cx<R>*>(a.bfilt);
+    const int tot = a.clines * Lc;
+    for (int e = tid; e < tot; e += nth) {
+      const int p = e / Lc, j = e % Lc;
+      Cx<R>* zl = z + (size_t)p * a.lp;
+      zl[j] = j < a.M ? zl[j] * chirp[j] : mk(R(0), R(0));
+    }
+    __syncthreads();
+    stockham<-1, R>(z, a, Lc);
+    for (int e = tid; e < tot; e += nth) {
+      const int p = e / Lc, j = e % Lc;
+      Cx<R>* zl = z + (size_t)p * a.lp;
+      zl[j] = zl[j] * bf[j];
+    }
+    __syncthreads();
+    stockham<1, R>(z, a, Lc);
+    const int tot2 = a.clines * a.M;
+    for (int e = tid; e < tot2; e += nth) {
+      const int p = e / a.M, j = e % a.M;
+      Cx<R>* zl = z + (size_t)p * a.lp;
+      zl[j] = zl[j] * chirp[j];
+    }
+    __syncthreads();
+  }
+
+  // ---- store ----
+  const R sc = a.scale_on ? R(a.scale) : R(1);
+  if (op == OP_C2C || op == OP_R2R_C) {
+    Cx<R>* out = reinterpret_cast<Cx<R>*>(a.out) + ooff;
+    const int tot = a.lines * a.n_out;
+    for (int e = tid; e < tot; e += nth) {
+      int i, k;
+      if (a.out_tfast) { i = e % a.lines; k = e / a.lines; } else { k = e % a.n_out; i = e / a.n_out; }
+      if (i >= nvalid) continue;
+      const Cx<R>* zl = z + (size_t)i * a.lp;
+      Cx<R> y = op == OP_C2C ? zl[k] : r2r_post(zl, a, k);
+      if (a.scale_on) y = scal(y, sc);
+      out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = y;
+    }
+  } else if (op == OP_R2C) {
+    Cx<R>* out = reinterpret_cast<Cx<R>*>(a.out) + ooff;
+    const int n = a.M, m = a.n_out;
+    const int tot = a.clines * m;
+    for (int e = tid; e < tot; e += nth) {
+      int p, k;
+      if (a.out_tfast) { p = e % a.clines; k = e / a.clines; } else { k = e % m; p = e / m; }
+      const Cx<R>* zl = z + (size_t)p * a.lp;
+      const Cx<R> f = zl[k], g = conj(zl[k == 0 ? 0 : n - k]);
+      Cx<R> A = scal(f + g, R(0.5));
+      Cx<R> B = scal(mul_mi(f - g), R(0.5));
+      if (a.scale_on) { A = scal(A, sc); B = scal(B, sc); }
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      if (i0 < nvalid) out[(int64_t)k * a.out_sa + (int64_t)i0 * a.out_st] = A;
+      if (i1 < nvalid) out[(int64_t)k * a.out_sa + (int64_t)i1 * a.out_st] = B;
+    }
+  } else {  // OP_C2R and OP_R2R_R: real output, two lines per complex line
+    R* out = reinterpret_cast<R*>(a.out) + ooff;
+    const int tot = a.clines * a.n_out;
+    for (int e = tid; e < tot; e += nth) {
+      int p, k;
+      if (a.out_tfast) { p = e % a.clines; k = e / a.clines; } else { k = e % a.n_out; p = e / a.n_out; }
+      const Cx<R>* zl = z + (size_t)p * a.lp;
+      Cx<R> y = op == OP_C2R ? zl[k] : r2r_post(zl, a, k);
+      if (a.scale_on) y = scal(y, sc);
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      if (i0 < nvalid) out[(int64_t)k * a.out_sa + (int64_t)i0 * a.out_st] = y.re;
+      if (i1 < nvalid) out[(int64_t)k * a.out_sa + (int64_t)i1 * a.out_st] = y.im;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Permuted copy (NoTransform passes): out (memory order) <- in (strided).
+// Bit-exact unless a scale is requested.
+// ---------------------------------------------------------------------------
+struct CopyArgs {
+  const void* in;
+  void* out;
+  int nd;
+  int64_t total;
+  int64_t osz[kMaxOuter];   // output sizes in output memory order (fastest first)
+  int64_t ist[kMaxOuter];   // input strides of those dims (elements)
+  int64_t ost[kMaxOuter];   // output strides of those dims (elements)
+  double scale;
+  int scale_on;
+  int real_is_double;       // element real type for scaling
+};
+
+template <typename E>
+__global__ void copy_kernel(const CopyArgs a) {
+  const E* in = reinterpret_cast<const E*>(a.in);
+  E* out = reinterpret_cast<E*>(a.out);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = e, io = 0, oo = 0;
+    for (int d = 0; d < a.nd; ++d) {
+      const int64_t idx = rem % a.osz[d];
+      rem /= a.osz[d];
+      io += idx * a.ist[d];
+      oo += idx * a.ost[d];
+    }
+    out[oo] = in[io];
+  }
+}
+
+}  // namespace pfgb

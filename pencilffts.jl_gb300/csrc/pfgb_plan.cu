@@ -1,0 +1,1036 @@
+// Host side of the C ABI: plan construction, pass scheduling, device tables
+// and execution.
+//
+// Reference behaviour restated here (paths within PencilFFTs.jl):
+//   - plan construction and per-dimension 1D plans: src/plans.jl:241-320,
+//     406-449, 523-553; global sizes and input type: src/global_params.jl:43-95
+//   - transform descriptors (length_output, binv, scale_factor):
+//     src/Transforms/{c2c,r2c,r2r,no_transform}.jl
+//   - execution order (forward left to right, backward right to left, ldiv!
+//     scaling): src/operations.jl:24-70, 154-257
+//   - output memory order reversed when permute_dims: src/plans.jl:503-521
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pencilfft_gb300.h"
+#include "pfgb_device.cuh"
+
+namespace pfgb {
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int fail_cuda(cudaError_t e, const char* what) {
+  return fail(PFGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PFGB_CUDA(call)                                                         \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess)                                                      \
+      return fail(PFGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int kMaxD = PFGB_MAX_DIMS + PFGB_MAX_EXTRA;
+constexpr int kMaxLc = 8192;  // longest line held in shared memory
+
+// ---------------------------------------------------------------------------
+// Layout of an array: logical sizes and memory order.
+// ---------------------------------------------------------------------------
+struct Layout {
+  int D = 0;
+  int64_t size[kMaxD] = {};
+  int perm[kMaxD] = {};  // perm[0] = fastest logical dim
+  int64_t pitch0 = 0;    // allocated extent of the fastest dim (>= its size)
+  int elt = 0;           // element bytes
+  bool complex = false;
+
+  int64_t stride(int d) const {
+    int64_t s = 1;
+    for (int q = 0; q < D; ++q) {
+      if (perm[q] == d) return s;
+      s *= (q == 0 ? pitch0 : size[perm[q]]);
+    }
+    return -1;
+  }
+  int64_t elems() const {
+    int64_t s = pitch0;
+    for (int q = 1; q < D; ++q) s *= size[perm[q]];
+    return s;
+  }
+  int64_t bytes() const { return elems() * elt; }
+  bool same_order(const Layout& o) const {
+    if (D != o.D) return false;
+    for (int q = 0; q < D; ++q)
+      if (perm[q] != o.perm[q]) return false;
+    return true;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// One executable pass.
+// ---------------------------------------------------------------------------
+enum PassKind { PK_TRANSFORM = 0, PK_COPY = 1 };
+
+struct Pass {
+  PassKind pk = PK_TRANSFORM;
+  int op = OP_C2C;
+  int r2r_kind = 0;
+  int sign = -1;
+  int axis = 0;
+  Layout lin, lout;
+  // DFT geometry
+  int M = 0, L = 0, nst = 0, rad[kMaxStages] = {};
+  const void* tw = nullptr;
+  const void* chirp = nullptr;
+  const void* bfilt = nullptr;
+  const void* r2rtw = nullptr;
+  // launch geometry
+  int lines = 1, clines = 1, bpl = 1, lp = 0, threads = 0;
+  size_t smem = 0;
+  bool zero_fill = false;
+  // buffer assignment: 0 = src, 1 = dst, 2 = scratch 1, 3 = scratch 2
+  int bin = 0, bout = 1;
+};
+
+struct Direction {
+  std::vector<Pass> passes;
+};
+
+}  // namespace pfgb
+
+struct pfgb_plan {
+  pfgb_plan_desc desc;
+  int N = 0, K = 0, D = 0;
+  int rb = 8;  // real bytes
+  bool inplace = false;
+  bool permute = true;
+  int64_t dims_in[pfgb::kMaxD] = {}, dims_out[pfgb::kMaxD] = {};
+  bool in_complex = false, out_complex = false;
+  double scale = 1.0;
+  pfgb::Layout in_layout, out_layout;  // user-visible input/output layouts
+  int64_t inplace_bytes = 0;
+  pfgb::Direction fwd, bwd;
+  void* scratch[2] = {nullptr, nullptr};
+  int64_t scratch_bytes[2] = {0, 0};
+  std::vector<void*> allocations;
+  std::map<std::string, void*> tables;
+  int device = 0;
+  bool query_only = false;  // plan analysed on the host only (no device memory)
+  // opt-in per-launch timing: (direction, pass index, start, stop)
+  bool timing = false;
+  struct Rec {
+    int dir, pass;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+};
+
+namespace pfgb {
+
+// ---------------------------------------------------------------------------
+// Transform descriptors (reference src/Transforms/*.jl)
+// ---------------------------------------------------------------------------
+static bool r2r_kind_supported(int k) { return k >= PFGB_DHT && k <= PFGB_RODFT11; }
+
+static int r2r_inverse(int k) {  // reference r2r.jl:103-131
+  switch (k) {
+    case PFGB_REDFT01: return PFGB_REDFT10;
+    case PFGB_REDFT10: return PFGB_REDFT01;
+    case PFGB_RODFT01: return PFGB_RODFT10;
+    case PFGB_RODFT10: return PFGB_RODFT01;
+    default: return k;
+  }
+}
+
+static int64_t length_output(int kind, bool even, int64_t n) {  // r2c.jl:74-75
+  if (kind == PFGB_RFFT) return n / 2 + 1;
+  if (kind == PFGB_BRFFT) return 2 * n - 1 - (even ? 1 : 0);
+  return n;
+}
+
+// Scale factor of a 1D transform evaluated on an input of length n
+// (reference c2c.jl:71, r2c.jl:103-111, r2r.jl:96-101, no_transform.jl:26).
+static double scale_1d(int kind, int r2r, bool even, int64_t n) {
+  switch (kind) {
+    case PFGB_FFT: case PFGB_BFFT: case PFGB_RFFT: return (double)n;
+    case PFGB_BRFFT: return (double)length_output(kind, even, n);
+    case PFGB_R2R:
+      if (r2r == PFGB_REDFT00) return 2.0 * (double)(n - 1);
+      if (r2r == PFGB_RODFT00) return 2.0 * (double)(n + 1);
+      if (r2r == PFGB_DHT) return (double)n;
+      return 2.0 * (double)n;
+    default: return 1.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host tables (long double), converted to the device real type.
+// ---------------------------------------------------------------------------
+typedef long double ld;
+static const ld kPi = 3.141592653589793238462643383279502884L;
+
+// exp(-i pi m / d), argument reduced exactly in integers.
+static std::complex<ld> expi_pi(int64_t m, int64_t d) {
+  const int64_t two_d = 2 * d;
+  m %= two_d;
+  if (m < 0) m += two_d;
+  const ld ang = kPi * (ld)m / (ld)d;
+  return std::complex<ld>(cosl(ang), -sinl(ang));
+}
+
+static void host_fft_pow2(std::vector<std::complex<ld>>& x, int sign) {
+  const size_t n = x.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(x[i], x[j]);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    for (size_t i = 0; i < n; i += len) {
+      for (size_t k = 0; k < len / 2; ++k) {
+        std::complex<ld> w = expi_pi(2 * (int64_t)k, (int64_t)len);  // exp(-2 pi i k/len)
+        if (sign > 0) w = std::conj(w);
+        std::complex<ld> u = x[i + k], v = x[i + k + len / 2] * w;
+        x[i + k] = u + v;
+        x[i + k + len / 2] = u - v;
+      }
+    }
+  }
+}
+
+static int upload_table(pfgb_plan* P, const std::string& key,
+                        const std::vector<std::complex<ld>>& v, const void** out) {
+  if (P->query_only) {
+    *out = nullptr;
+    return PFGB_OK;
+  }
+  auto it = P->tables.find(key);
+  if (it != P->tables.end()) {
+    *out = it->second;
+    return PFGB_OK;
+  }
+  void* d = nullptr;
+  size_t bytes = v.size() * 2 * P->rb;
+  PFGB_CUDA(cudaMalloc(&d, std::max<size_t>(bytes, 16)));
+  if (P->rb == 8) {
+    std::vector<double> h(2 * v.size());
+    for (size_t i = 0; i < v.size(); ++i) { h[2 * i] = (double)v[i].real(); h[2 * i + 1] = (double)v[i].imag(); }
+    PFGB_CUDA(cudaMemcpy(d, h.data(), bytes, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> h(2 * v.size());
+    for (size_t i = 0; i < v.size(); ++i) { h[2 * i] = (float)v[i].real(); h[2 * i + 1] = (float)v[i].imag(); }
+    PFGB_CUDA(cudaMemcpy(d, h.data(), bytes, cudaMemcpyHostToDevice));
+  }
+  P->tables[key] = d;
+  *out = d;
+  return PFGB_OK;
+}
+
+// Radix plan for a DFT length: returns false if a prime factor > 13 remains.
+static bool factor_radices(int n, std::vector<int>& rad) {
+  rad.clear();
+  int e = 0;
+  while (n % 2 == 0) { n /= 2; ++e; }
+  static const int odd[] = {3, 5, 7, 11, 13};
+  std::vector<int> odds;
+  for (int p : odd)
+    while (n % p == 0) { n /= p; odds.push_back(p); }
+  if (n != 1) return false;
+  if (e > 0) {
+    const int s = (e + 3) / 4;
+    for (int i = 0; i < s; ++i) {
+      const int ei = e / s + (i < e % s ? 1 : 0);
+      rad.push_back(1 << ei);
+    }
+  }
+  for (int p : odds) rad.push_back(p);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Pass preparation: DFT geometry, tables, launch shape.
+// ---------------------------------------------------------------------------
+static int prepare_core(pfgb_plan* P, Pass& ps, int M) {
+  ps.M = M;
+  std::vector<int> rad;
+  int Lc = M;
+  if (!factor_radices(M, rad)) {
+    int L = 1;
+    while (L < 2 * M - 1) L <<= 1;
+    ps.L = L;
+    Lc = L;
+    factor_radices(L, rad);
+  }
+  if (Lc > kMaxLc)
+    return fail(PFGB_ERR_UNSUPPORTED, "transform length " + std::to_string(M) +
+                                          " exceeds the longest supported line (core length " +
+                                          std::to_string(Lc) + " > 8192)");
+  ps.nst = (int)rad.size();
+  for (int i = 0; i < ps.nst; ++i) ps.rad[i] = rad[i];
+  // core twiddles exp(-2 pi i m / Lc)
+  {
+    std::vector<std::complex<ld>> t(Lc);
+    for (int m = 0; m < Lc; ++m) t[m] = expi_pi(2 * (int64_t)m, Lc);
+    int rc = upload_table(P, "tw" + std::to_string(Lc), t, &ps.tw);
+    if (rc) return rc;
+  }
+  if (ps.L > 0) {
+    const int L = ps.L;
+    std::vector<std::complex<ld>> c(M), b(L, std::complex<ld>(0, 0));
+    for (int j = 0; j < M; ++j) {
+      const int64_t jj = ((int64_t)j * j) % (2 * (int64_t)M);
+      c[j] = expi_pi(jj, M);  // exp(-i pi j^2 / M)
+    }
+    for (int j = 0; j < M; ++j) b[j] = std::conj(c[j]);
+    for (int j = 1; j < M; ++j) b[L - j] = std::conj(c[j]);
+    std::vector<std::complex<ld>> cs(M), bs(b);
+    if (ps.sign > 0) {
+      for (int j = 0; j < M; ++j) cs[j] = std::conj(c[j]);
+      for (auto& v : bs) v = std::conj(v);
+    } else {
+      cs = c;
+    }
+    host_fft_pow2(bs, -1);
+    for (auto& v : bs) v /= (ld)L;
+    const std::string k = std::to_string(M) + (ps.sign > 0 ? "+" : "-");
+    int rc = upload_table(P, "chirp" + k, cs, &ps.chirp);
+    if (rc) return rc;
+    rc = upload_table(P, "bfilt" + k, bs, &ps.bfilt);
+    if (rc) return rc;
+  }
+  return PFGB_OK;
+}
+
+static int prepare_pass(pfgb_plan* P, Pass& ps) {
+  if (ps.pk == PK_COPY) {
+    ps.threads = 256;
+    return PFGB_OK;
+  }
+  const int a = ps.axis;
+  const int64_t n_in = ps.lin.size[a], n_out = ps.lout.size[a];
+  if (n_in > kMaxLc * 2 || n_out > kMaxLc * 2)
+    return fail(PFGB_ERR_UNSUPPORTED, "line too long");
+  int M = 0;
+  switch (ps.op) {
+    case OP_C2C: M = (int)n_in; break;
+    case OP_R2C: M = (int)n_in; break;
+    case OP_C2R: M = (int)n_out; break;
+    default: {
+      const int n = (int)n_in;
+      switch (ps.r2r_kind) {
+        case K_DHT: M = n; break;
+        case K_REDFT00:
+          if (n < 2) return fail(PFGB_ERR_ARGUMENT, "REDFT00 requires a length of at least 2");
+          M = 2 * (n - 1);
+          break;
+        case K_RODFT00: M = 2 * (n + 1); break;
+        default: M = 2 * n; break;
+      }
+      ps.sign = -1;
+      if (ps.r2r_kind != K_DHT) {
+        std::vector<std::complex<ld>> t(4 * (size_t)n + 2);
+        for (int m = 0; m < 4 * n + 2; ++m) t[m] = expi_pi(m, 4 * (int64_t)n);
+        int rc = upload_table(P, "r2r" + std::to_string(n), t, &ps.r2rtw);
+        if (rc) return rc;
+      }
+      break;
+    }
+  }
+  int rc = prepare_core(P, ps, M);
+  if (rc) return rc;
+  const int Lc = ps.L > 0 ? ps.L : ps.M;
+  int rmin = 64;
+  for (int i = 0; i < ps.nst; ++i) rmin = std::min(rmin, ps.rad[i]);
+  ps.bpl = Lc / rmin;
+  ps.lp = Lc;
+  const bool packed = ps.op == OP_R2C || ps.op == OP_C2R || ps.op == OP_R2R_R;
+  const size_t cbytes = 2 * (size_t)P->rb;
+  // complex lines per CTA: bounded by 1024 threads and the shared-memory budget
+  const size_t smem_budget = 96 * 1024;
+  int cl_thr = std::max(1, 1024 / ps.bpl);
+  int cl_smem = (int)std::max<size_t>(1, smem_budget / (Lc * cbytes));
+  int target = 16;  // aim at 16 array lines per tile (coalescing of strided axes)
+  int cl = std::min({cl_thr, cl_smem, packed ? target / 2 : target});
+  // threads: at least the butterflies, at least 128 for the load/store loops
+  if (cl < 1) cl = 1;
+  ps.clines = cl;
+  ps.lines = packed ? 2 * cl : cl;
+  int th = cl * ps.bpl;
+  th = std::max(th, 128);
+  th = std::min(th, 1024);
+  th = (th + 31) / 32 * 32;
+  ps.threads = th;
+  ps.smem = (size_t)cl * ps.lp * cbytes;
+  if (ps.smem > 200 * 1024)
+    return fail(PFGB_ERR_UNSUPPORTED, "line does not fit in shared memory");
+  ps.zero_fill = ps.L > 0 || (ps.op == OP_R2R_C || ps.op == OP_R2R_R);
+  return PFGB_OK;
+}
+
+// Fills the kernel arguments of a transform pass for given buffers.
+static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* out, bool scale_on,
+                     PassArgs& A, int64_t& grid) {
+  std::memset(&A, 0, sizeof(A));
+  A.in = in;
+  A.out = out;
+  A.tw = ps.tw;
+  A.chirp = ps.chirp;
+  A.bfilt = ps.bfilt;
+  A.r2rtw = ps.r2rtw;
+  A.op = ps.op;
+  A.r2r_kind = ps.r2r_kind;
+  A.sign = ps.sign;
+  A.scale_on = scale_on ? 1 : 0;
+  A.scale = scale_on ? 1.0 / P->scale : 1.0;
+  const int a = ps.axis;
+  A.n_in = (int)ps.lin.size[a];
+  A.n_out = (int)ps.lout.size[a];
+  A.M = ps.M;
+  A.L = ps.L;
+  A.nst = ps.nst;
+  for (int i = 0; i < ps.nst; ++i) A.rad[i] = ps.rad[i];
+  A.lines = ps.lines;
+  A.clines = ps.clines;
+  A.bpl = ps.bpl;
+  A.lp = ps.lp;
+  A.zero_fill = ps.zero_fill ? 1 : 0;
+  // strides in elements of each side
+  const int D = ps.lin.D;
+  A.in_sa = ps.lin.stride(a);
+  A.out_sa = ps.lout.stride(a);
+  const bool a_fast_in = ps.lin.perm[0] == a;
+  const bool a_fast_out = ps.lout.perm[0] == a;
+  int t = -1;
+  if (!a_fast_in) {
+    t = ps.lin.perm[0];
+    if (!a_fast_out && ps.lout.perm[0] != t)
+      return fail(PFGB_ERR_UNSUPPORTED, "internal: incompatible pass layouts");
+  } else if (!a_fast_out) {
+    t = ps.lout.perm[0];
+  } else if (D > 1) {
+    t = ps.lin.perm[1];
+  }
+  if (t >= 0) {
+    A.nt = ps.lin.size[t];
+    A.in_st = ps.lin.stride(t);
+    A.out_st = ps.lout.stride(t);
+  } else {
+    A.nt = 1;
+    A.in_st = A.out_st = 0;
+  }
+  A.in_tfast = (t >= 0 && A.in_st == 1) ? 1 : 0;
+  A.out_tfast = (t >= 0 && A.out_st == 1) ? 1 : 0;
+  A.ntiles = (A.nt + ps.lines - 1) / ps.lines;
+  int no = 0;
+  int64_t nblocks = A.ntiles;
+  for (int q = 0; q < D; ++q) {  // outer dims in input memory order
+    const int d = ps.lin.perm[q];
+    if (d == a || d == t) continue;
+    if (no >= kMaxOuter) return fail(PFGB_ERR_UNSUPPORTED, "too many dimensions");
+    A.osz[no] = ps.lin.size[d];
+    A.in_so[no] = ps.lin.stride(d);
+    A.out_so[no] = ps.lout.stride(d);
+    nblocks *= ps.lin.size[d];
+    ++no;
+  }
+  A.nouter = no;
+  grid = nblocks;
+  return PFGB_OK;
+}
+
+static int make_copy_args(const Pass& ps, const void* in, void* out, CopyArgs& C) {
+  std::memset(&C, 0, sizeof(C));
+  C.in = in;
+  C.out = out;
+  const int D = ps.lout.D;
+  C.nd = D;
+  int64_t total = 1;
+  for (int q = 0; q < D; ++q) {
+    const int d = ps.lout.perm[q];
+    C.osz[q] = ps.lout.size[d];
+    C.ist[q] = ps.lin.stride(d);
+    C.ost[q] = ps.lout.stride(d);
+    total *= ps.lout.size[d];
+  }
+  C.total = total;
+  return PFGB_OK;
+}
+
+// Launchers (pfgb_kernels.cu)
+int launch_pass(int real_bytes, const PassArgs& A, int64_t grid, int threads, size_t smem,
+                cudaStream_t s);
+int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Schedule: build the passes of one direction and assign buffers.
+// ---------------------------------------------------------------------------
+static Layout natural_layout(const pfgb_plan* P, const int64_t* sizes, bool complex, int64_t pitch0) {
+  Layout L;
+  L.D = P->D;
+  for (int d = 0; d < P->N; ++d) L.size[d] = sizes[d];
+  for (int e = 0; e < P->K; ++e) L.size[P->N + e] = P->desc.extra_dims[e];
+  for (int q = 0; q < L.D; ++q) L.perm[q] = q;
+  L.pitch0 = pitch0 > 0 ? pitch0 : L.size[L.perm[0]];
+  L.complex = complex;
+  L.elt = complex ? 2 * P->rb : P->rb;
+  return L;
+}
+
+static Layout final_layout(const pfgb_plan* P, const int64_t* sizes, bool complex) {
+  Layout L = natural_layout(P, sizes, complex, 0);
+  if (P->permute) {
+    for (int q = 0; q < P->N; ++q) L.perm[q] = P->N - 1 - q;
+    L.pitch0 = L.size[L.perm[0]];
+  }
+  return L;
+}
+
+static bool layouts_differ(const pfgb_plan* P) { return P->permute && P->N >= 2; }
+
+// In-place safety of a pass: every tile writes exactly the bytes it read.
+static bool inplace_ok(const Pass& ps) {
+  if (!ps.lin.same_order(ps.lout)) return false;
+  const int a = ps.axis;
+  for (int d = 0; d < ps.lin.D; ++d) {
+    if (d == a) continue;
+    if (ps.lin.stride(d) * ps.lin.elt != ps.lout.stride(d) * ps.lout.elt) return false;
+  }
+  if (ps.lin.perm[0] == a) {
+    return ps.lin.pitch0 * ps.lin.elt == ps.lout.pitch0 * ps.lout.elt;
+  }
+  return ps.lin.elt == ps.lout.elt && ps.lin.size[a] == ps.lout.size[a];
+}
+
+struct Step {  // one transform of the reference's per-dimension loop
+  int axis, op, r2r, sign;
+};
+
+static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t cap_src,
+                           int64_t cap_dst, int64_t pitch_real) {
+  const int N = P->N;
+  const pfgb_plan_desc& d = P->desc;
+  // Element type and sizes along the chain.
+  int64_t sizes[kMaxD];
+  bool cplx;
+  std::vector<Step> steps;
+  if (forward) {
+    for (int n = 0; n < N; ++n) sizes[n] = P->dims_in[n];
+    cplx = P->in_complex;
+    for (int n = 0; n < N; ++n) {
+      Step s{n, -1, 0, -1};
+      switch (d.kind[n]) {
+        case PFGB_FFT: s.op = OP_C2C; s.sign = -1; break;
+        case PFGB_BFFT: s.op = OP_C2C; s.sign = 1; break;
+        case PFGB_RFFT: s.op = OP_R2C; s.sign = -1; break;
+        case PFGB_BRFFT: s.op = OP_C2R; s.sign = 1; break;
+        case PFGB_R2R: s.op = OP_R2R_C; s.r2r = d.r2r_kind[n]; break;
+        default: continue;
+      }
+      steps.push_back(s);
+    }
+  } else {
+    for (int n = 0; n < N; ++n) sizes[n] = P->dims_out[n];
+    cplx = P->out_complex;
+    for (int n = N - 1; n >= 0; --n) {
+      Step s{n, -1, 0, -1};
+      switch (d.kind[n]) {  // binv (reference c2c.jl:58-61, r2c.jl:98-101, r2r.jl:103-131)
+        case PFGB_FFT: s.op = OP_C2C; s.sign = 1; break;
+        case PFGB_BFFT: s.op = OP_C2C; s.sign = -1; break;
+        case PFGB_RFFT: s.op = OP_C2R; s.sign = 1; break;
+        case PFGB_BRFFT: s.op = OP_R2C; s.sign = -1; break;
+        case PFGB_R2R: s.op = OP_R2R_C; s.r2r = r2r_inverse(d.r2r_kind[n]); break;
+        default: continue;
+      }
+      steps.push_back(s);
+    }
+  }
+  const bool change = layouts_differ(P);
+  // index of the step that performs the layout change
+  int tx = -1;
+  if (change) {
+    for (size_t i = 0; i < steps.size(); ++i)
+      if (steps[i].axis == 0 || steps[i].axis == N - 1) { tx = (int)i; break; }
+  }
+  std::vector<Pass> passes;
+  auto mk_layout = [&](bool fin, const int64_t* sz, bool cx, int64_t pitch) {
+    // "fin" = final (output-pencil) order in the forward direction
+    if (fin) return final_layout(P, sz, cx);
+    return natural_layout(P, sz, cx, pitch);
+  };
+  // In the forward direction the data starts in natural order and ends in the
+  // final order; backward is the reverse.
+  bool start_fin = !forward;
+  bool end_fin = forward;
+  if (!change) start_fin = end_fin = false;
+  const int64_t pitch_start = forward ? pitch_real : 0;
+  const int64_t pitch_end = forward ? 0 : pitch_real;
+  Layout cur = mk_layout(start_fin, sizes, cplx, pitch_start);
+  bool cur_fin = start_fin;
+  if (change && tx < 0) {
+    // no step can re-layout: a permuted copy first
+    Pass c;
+    c.pk = PK_COPY;
+    c.lin = cur;
+    c.lout = mk_layout(end_fin, sizes, cplx, 0);
+    c.axis = -1;
+    passes.push_back(c);
+    cur = c.lout;
+    cur_fin = end_fin;
+  }
+  for (size_t i = 0; i < steps.size(); ++i) {
+    const Step& s = steps[i];
+    Pass ps;
+    ps.pk = PK_TRANSFORM;
+    ps.axis = s.axis;
+    ps.sign = s.sign;
+    ps.r2r_kind = s.r2r;
+    ps.op = s.op;
+    if (s.op == OP_R2R_C && !cplx) ps.op = OP_R2R_R;
+    ps.lin = cur;
+    int64_t nsz[kMaxD];
+    for (int q = 0; q < N; ++q) nsz[q] = sizes[q];
+    bool ncx = cplx;
+    if (s.op == OP_R2C) {
+      nsz[s.axis] = sizes[s.axis] / 2 + 1;
+      ncx = true;
+    } else if (s.op == OP_C2R) {
+      // output length: forward BRFFT uses even_output; backward RFFT^-1 restores dims_in
+      nsz[s.axis] = forward ? length_output(PFGB_BRFFT, d.brfft_even[s.axis] != 0, sizes[s.axis])
+                            : P->dims_in[s.axis];
+      ncx = false;
+    }
+    const bool last = i + 1 == steps.size();
+    const bool out_fin = ((int)i >= tx && tx >= 0) ? end_fin : cur_fin;
+    const int64_t pitch = (last && !out_fin) ? pitch_end : 0;
+    ps.lout = mk_layout(out_fin, nsz, ncx, pitch && !ncx ? pitch : 0);
+    passes.push_back(ps);
+    cur = ps.lout;
+    cur_fin = out_fin;
+    for (int q = 0; q < N; ++q) sizes[q] = nsz[q];
+    cplx = ncx;
+  }
+  if (passes.empty()) {
+    if (!P->inplace) {
+      Pass c;
+      c.pk = PK_COPY;
+      c.lin = cur;
+      c.lout = cur;
+      c.axis = -1;
+      passes.push_back(c);
+    }
+  }
+  // Buffer assignment (brute force over {dst, s1, s2} for intermediates).
+  const int m = (int)passes.size();
+  if (m == 0) {
+    dir.passes.clear();
+    return PFGB_OK;
+  }
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const int mm = (int)passes.size();
+    int best_cost_ok = 0;
+    int64_t best_cost = -1;
+    std::vector<int> best;
+    std::vector<int> asg(mm);
+    int64_t combos = 1;
+    for (int i = 0; i < mm - 1; ++i) combos *= 3;
+    for (int64_t c = 0; c < combos; ++c) {
+      int64_t cc = c;
+      for (int i = 0; i < mm - 1; ++i) { asg[i] = 1 + (int)(cc % 3); cc /= 3; }
+      asg[mm - 1] = 1;
+      bool ok = true;
+      int64_t need[4] = {0, 0, 0, 0};
+      int prev = P->inplace ? 1 : 0;  // in-place plans read the dst buffer
+      for (int i = 0; i < mm && ok; ++i) {
+        const int bi = prev, bo = asg[i];
+        const Pass& ps = passes[i];
+        const bool ip = ps.pk == PK_COPY ? ps.lin.same_order(ps.lout) && ps.lin.pitch0 == ps.lout.pitch0 && ps.lin.elt == ps.lout.elt
+                                         : inplace_ok(ps);
+        if (bi == bo && !ip) ok = false;
+        need[bo] = std::max(need[bo], ps.lout.bytes());
+        prev = bo;
+      }
+      if (!ok) continue;
+      if (need[1] > cap_dst) continue;
+      const int64_t cost = need[2] + need[3];
+      if (best_cost < 0 || cost < best_cost) {
+        best_cost = cost;
+        best = asg;
+        best_cost_ok = 1;
+      }
+    }
+    if (best_cost_ok) {
+      int prev = P->inplace ? 1 : 0;
+      for (int i = 0; i < mm; ++i) {
+        passes[i].bin = prev;
+        passes[i].bout = best[i];
+        prev = best[i];
+        if (best[i] >= 2) {
+          const int s = best[i] - 2;
+          P->scratch_bytes[s] = std::max(P->scratch_bytes[s], passes[i].lout.bytes());
+        }
+      }
+      dir.passes = passes;
+      return PFGB_OK;
+    }
+    // infeasible: append an identity copy so the data can return to dst
+    Pass c;
+    c.pk = PK_COPY;
+    c.lin = passes.back().lout;
+    c.lout = passes.back().lout;
+    c.axis = -1;
+    passes.push_back(c);
+  }
+  (void)cap_src;
+  return fail(PFGB_ERR_UNSUPPORTED, "internal: no buffer assignment for this plan");
+}
+
+static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* src,
+                   cudaStream_t s, bool normalise, int dsign) {
+  const int m = (int)dir.passes.size();
+  if (m == 0) return PFGB_OK;
+  int last_tr = -1;
+  for (int i = 0; i < m; ++i)
+    if (dir.passes[i].pk == PK_TRANSFORM) last_tr = i;
+  for (int i = 0; i < m; ++i) {
+    const Pass& ps = dir.passes[i];
+    auto buf = [&](int b) -> void* {
+      switch (b) {
+        case 0: return const_cast<void*>(src);
+        case 1: return dst;
+        default: return P->scratch[b - 2];
+      }
+    };
+    const void* in = buf(ps.bin);
+    void* out = buf(ps.bout);
+    if (ps.pk == PK_COPY && in == out && ps.lin.same_order(ps.lout)) continue;
+    pfgb_plan::Rec rec{dsign, i, nullptr, nullptr};
+    if (P->timing) {
+      PFGB_CUDA(cudaEventCreate(&rec.a));
+      PFGB_CUDA(cudaEventCreate(&rec.b));
+      PFGB_CUDA(cudaEventRecord(rec.a, s));
+    }
+    if (ps.pk == PK_COPY) {
+      CopyArgs C;
+      make_copy_args(ps, in, out, C);
+      int rc = launch_copy(ps.lout.elt, C, s);
+      if (rc) return rc;
+    } else {
+      PassArgs A;
+      int64_t grid = 0;
+      int rc = make_args(P, ps, in, out, normalise && i == last_tr, A, grid);
+      if (rc) return rc;
+      rc = launch_pass(P->rb, A, grid, ps.threads, ps.smem, s);
+      if (rc) return rc;
+    }
+    if (P->timing) {
+      PFGB_CUDA(cudaEventRecord(rec.b, s));
+      P->recs.push_back(rec);
+    }
+  }
+  return PFGB_OK;
+}
+
+}  // namespace pfgb
+
+using namespace pfgb;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* pfgb_version(void) { return "pencilfft_gb300 0.1.0 (sm_103a)"; }
+
+int pfgb_last_error(char* buf, size_t n) {
+  const std::string& e = g_last_error;
+  if (buf && n > 0) {
+    size_t k = std::min(n - 1, e.size());
+    std::memcpy(buf, e.data(), k);
+    buf[k] = 0;
+  }
+  return (int)e.size();
+}
+
+static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_only) {
+  g_last_error.clear();
+  if (!desc || !out) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  const pfgb_plan_desc& d = *desc;
+  if (d.ndims < 1 || d.ndims > PFGB_MAX_DIMS)
+    return fail(PFGB_ERR_ARGUMENT, "ndims must be in [1, " + std::to_string(PFGB_MAX_DIMS) + "]");
+  if (d.n_extra < 0 || d.n_extra > PFGB_MAX_EXTRA)
+    return fail(PFGB_ERR_ARGUMENT, "too many extra_dims");
+  if (d.real_bytes != 4 && d.real_bytes != 8)
+    return fail(PFGB_ERR_ARGUMENT, "real type must be Float32 (4) or Float64 (8)");
+  if (d.precision_mode != 0)
+    return fail(PFGB_ERR_UNSUPPORTED, "precision mode not available in this build");
+  for (int n = 0; n < d.ndims; ++n) {
+    if (d.dims[n] < 1) return fail(PFGB_ERR_ARGUMENT, "dimensions must be positive");
+    if (d.kind[n] < PFGB_FFT || d.kind[n] > PFGB_NOTRANSFORM)
+      return fail(PFGB_ERR_ARGUMENT, "unknown transform kind");
+    if (d.kind[n] == PFGB_R2R && !r2r_kind_supported(d.r2r_kind[n]))
+      return fail(PFGB_ERR_ARGUMENT, "unsupported r2r transform kind: " + std::to_string(d.r2r_kind[n]));
+  }
+  for (int e = 0; e < d.n_extra; ++e)
+    if (d.extra_dims[e] < 1) return fail(PFGB_ERR_ARGUMENT, "extra dimensions must be positive");
+  // reference global_params.jl:57-60: no mix of in-place and out-of-place
+  for (int n = 1; n < d.ndims; ++n)
+    if ((d.inplace[n] != 0) != (d.inplace[0] != 0))
+      return fail(PFGB_ERR_ARGUMENT, "cannot combine in-place and out-of-place transforms");
+
+  pfgb_plan* P = new pfgb_plan();
+  P->query_only = query_only;
+  P->desc = d;
+  P->N = d.ndims;
+  P->K = d.n_extra;
+  P->D = P->N + P->K;
+  P->rb = d.real_bytes;
+  P->inplace = d.inplace[0] != 0;
+  P->permute = d.permute_dims != 0;
+  if (!query_only) cudaGetDevice(&P->device);
+  // input element type (reference global_params.jl:81-95)
+  bool in_cx = false, decided = false;
+  for (int n = 0; n < P->N && !decided; ++n) {
+    switch (d.kind[n]) {
+      case PFGB_FFT: case PFGB_BFFT: case PFGB_BRFFT: in_cx = true; decided = true; break;
+      case PFGB_RFFT: in_cx = false; decided = true; break;
+      default: break;
+    }
+  }
+  P->in_complex = in_cx;
+  // walk the chain: sizes, element types (reference global_params.jl:50-62)
+  bool cx = in_cx;
+  double scale = 1.0;
+  for (int n = 0; n < P->N; ++n) {
+    const int k = d.kind[n];
+    if ((k == PFGB_FFT || k == PFGB_BFFT || k == PFGB_BRFFT) && !cx) {
+      delete P;
+      return fail(PFGB_ERR_ARGUMENT, "invalid input data type for transform along dimension " +
+                                         std::to_string(n + 1) + ": expected complex data");
+    }
+    if (k == PFGB_RFFT && cx) {
+      delete P;
+      return fail(PFGB_ERR_ARGUMENT, "invalid input data type for RFFT along dimension " +
+                                         std::to_string(n + 1) + ": expected real data");
+    }
+    P->dims_in[n] = d.dims[n];
+    P->dims_out[n] = length_output(k, d.brfft_even[n] != 0, d.dims[n]);
+    if (P->dims_out[n] < 1) {
+      delete P;
+      return fail(PFGB_ERR_ARGUMENT, "empty output dimension");
+    }
+    if (k == PFGB_RFFT) cx = true;
+    if (k == PFGB_BRFFT) cx = false;
+    // backward scale of this dimension (reference plans.jl:540-546): binv of
+    // the transform evaluated on the forward output length
+    int kb = k, rb = d.r2r_kind[n];
+    bool eb = false;
+    if (k == PFGB_FFT) kb = PFGB_BFFT;
+    else if (k == PFGB_BFFT) kb = PFGB_FFT;
+    else if (k == PFGB_RFFT) { kb = PFGB_BRFFT; eb = d.dims[n] % 2 == 0; }
+    else if (k == PFGB_BRFFT) kb = PFGB_RFFT;
+    else if (k == PFGB_R2R) rb = r2r_inverse(d.r2r_kind[n]);
+    scale *= scale_1d(kb, rb, eb, P->dims_out[n]);
+  }
+  P->out_complex = cx;
+  P->scale = scale;
+  // in-place RFFT! uses a padded real view (reference multiarrays_r2c.jl:69-79)
+  int64_t pitch_real = 0;
+  const bool inplace_rfft = P->inplace && d.kind[0] == PFGB_RFFT;
+  const bool inplace_brfft = P->inplace && d.kind[P->N - 1] == PFGB_BRFFT;
+  if (inplace_rfft) pitch_real = 2 * (d.dims[0] / 2 + 1);
+  if (inplace_brfft) {
+    delete P;
+    return fail(PFGB_ERR_UNSUPPORTED, "in-place BRFFT! plans are not supported (the reference has no "
+                                      "container for them either)");
+  }
+  P->in_layout = natural_layout(P, P->dims_in, in_cx, inplace_rfft ? pitch_real : 0);
+  P->out_layout = final_layout(P, P->dims_out, cx);
+  // capacity of the aliased in-place buffer: largest array along the chain
+  if (P->inplace) {
+    if (in_cx != cx && !inplace_rfft) {
+      delete P;
+      return fail(PFGB_ERR_UNSUPPORTED, "in-place plans need the same element type throughout");
+    }
+    P->inplace_bytes = std::max(P->in_layout.bytes(), P->out_layout.bytes());
+  }
+  const int64_t cap_dst_f = P->inplace ? P->inplace_bytes : P->out_layout.bytes();
+  const int64_t cap_dst_b = P->inplace ? P->inplace_bytes : P->in_layout.bytes();
+  int rc = build_direction(P, true, P->fwd, P->in_layout.bytes(), cap_dst_f, pitch_real);
+  if (!rc) rc = build_direction(P, false, P->bwd, P->out_layout.bytes(), cap_dst_b, pitch_real);
+  for (auto* dir : {&P->fwd, &P->bwd})
+    for (auto& ps : dir->passes)
+      if (!rc) rc = prepare_pass(P, ps);
+  if (!rc && !query_only) {
+    for (int s = 0; s < 2; ++s) {
+      if (P->scratch_bytes[s] > 0) {
+        cudaError_t e = cudaMalloc(&P->scratch[s], P->scratch_bytes[s]);
+        if (e != cudaSuccess) {
+          rc = fail(PFGB_ERR_ALLOC, std::string("scratch allocation failed: ") + cudaGetErrorString(e));
+          break;
+        }
+      }
+    }
+  }
+  if (rc) {
+    pfgb_plan_destroy(P);
+    return rc;
+  }
+  *out = P;
+  return PFGB_OK;
+}
+
+int pfgb_plan_create(const pfgb_plan_desc* desc, pfgb_plan** out) {
+  return plan_build(desc, out, false);
+}
+
+int pfgb_plan_query(const pfgb_plan_desc* desc, pfgb_plan_info* info) {
+  if (!info) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  pfgb_plan* P = nullptr;
+  int rc = plan_build(desc, &P, true);
+  if (rc) return rc;
+  rc = pfgb_plan_info_get(P, info);
+  pfgb_plan_destroy(P);
+  return rc;
+}
+
+static void clear_records(pfgb_plan* P) {
+  for (auto& r : P->recs) {
+    if (r.a) cudaEventDestroy(r.a);
+    if (r.b) cudaEventDestroy(r.b);
+  }
+  P->recs.clear();
+}
+
+int pfgb_plan_set_timing(pfgb_plan* P, int on) {
+  if (!P) return fail(PFGB_ERR_ARGUMENT, "null plan");
+  clear_records(P);
+  P->timing = on != 0 && !P->query_only;
+  return PFGB_OK;
+}
+
+int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
+  if (!P || !n || (max > 0 && !out)) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  std::vector<pfgb_pass_timing> acc;
+  auto entry = [&](int dir, int pass) -> pfgb_pass_timing& {
+    for (auto& e : acc)
+      if (e.direction == dir && e.pass == pass) return e;
+    pfgb_pass_timing e;
+    std::memset(&e, 0, sizeof(e));
+    e.direction = dir;
+    e.pass = pass;
+    const Pass& ps = (dir > 0 ? P->fwd : P->bwd).passes[pass];
+    e.axis = ps.axis;
+    e.op = ps.pk == PK_COPY ? -1 : ps.op;
+    e.bytes_per_launch = ps.lin.bytes() + ps.lout.bytes();
+    const char* kname = ps.pk == PK_COPY ? "copy_kernel" : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
+    std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);
+    acc.push_back(e);
+    return acc.back();
+  };
+  for (auto& r : P->recs) {
+    PFGB_CUDA(cudaEventSynchronize(r.b));
+    float ms = 0.f;
+    PFGB_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+    pfgb_pass_timing& e = entry(r.dir, r.pass);
+    e.launches += 1;
+    e.total_ms += ms;
+  }
+  clear_records(P);
+  *n = (int)acc.size();
+  for (int i = 0; i < std::min(max, (int)acc.size()); ++i) out[i] = acc[i];
+  return PFGB_OK;
+}
+
+int pfgb_plan_destroy(pfgb_plan* P) {
+  if (!P) return PFGB_OK;
+  clear_records(P);
+  for (int s = 0; s < 2; ++s)
+    if (P->scratch[s]) cudaFree(P->scratch[s]);
+  for (auto& kv : P->tables) cudaFree(kv.second);
+  delete P;
+  return PFGB_OK;
+}
+
+int pfgb_plan_info_get(const pfgb_plan* P, pfgb_plan_info* info) {
+  if (!P || !info) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  std::memset(info, 0, sizeof(*info));
+  info->ndims = P->N;
+  for (int n = 0; n < P->N; ++n) {
+    info->dims_in[n] = P->dims_in[n];
+    info->dims_out[n] = P->dims_out[n];
+  }
+  for (int q = 0; q < P->N; ++q) info->perm_out[q] = P->out_layout.perm[q];
+  info->eltype_in_complex = P->in_complex;
+  info->eltype_out_complex = P->out_complex;
+  info->real_bytes = P->rb;
+  info->inplace = P->inplace;
+  info->scale_factor = P->scale;
+  info->input_bytes = P->in_layout.bytes();
+  info->output_bytes = P->out_layout.bytes();
+  info->inplace_bytes = P->inplace_bytes;
+  info->scratch_bytes = P->scratch_bytes[0] + P->scratch_bytes[1];
+  info->n_passes_forward = (int)P->fwd.passes.size();
+  info->n_passes_backward = (int)P->bwd.passes.size();
+  return PFGB_OK;
+}
+
+static int check_buffers(pfgb_plan* P, void* dst, const void* src, bool forward) {
+  if (!P) return fail(PFGB_ERR_ARGUMENT, "null plan");
+  if (!dst || !src) return fail(PFGB_ERR_ARGUMENT, "null array");
+  if (P->inplace) {
+    // reference operations.jl:98-108
+    if (dst != src) return fail(PFGB_ERR_ARGUMENT, "input and output arrays for in-place plan must be the same");
+  } else {
+    // reference operations.jl:87-96 (Base.mightalias)
+    const int64_t bi = forward ? P->in_layout.bytes() : P->out_layout.bytes();
+    const int64_t bo = forward ? P->out_layout.bytes() : P->in_layout.bytes();
+    const char* s = (const char*)src;
+    const char* t = (const char*)dst;
+    if (s < t + bo && t < s + bi) return fail(PFGB_ERR_ARGUMENT, "out-of-place plan applied to aliased data");
+  }
+  return PFGB_OK;
+}
+
+int pfgb_forward(pfgb_plan* P, void* dst, const void* src, void* stream) {
+  int rc = check_buffers(P, dst, src, true);
+  if (rc) return rc;
+  return execute(P, P->fwd, dst, src, (cudaStream_t)stream, false, 1);
+}
+
+int pfgb_backward(pfgb_plan* P, void* dst, const void* src, void* stream, int normalise) {
+  int rc = check_buffers(P, dst, src, false);
+  if (rc) return rc;
+  return execute(P, P->bwd, dst, src, (cudaStream_t)stream, normalise != 0, -1);
+}
+
+int pfgb_execute_many(pfgb_plan* P, int direction, int normalise, void* const* dst,
+                      const void* const* src, int n, void* stream) {
+  if (!P) return fail(PFGB_ERR_ARGUMENT, "null plan");
+  if (n < 0 || (n > 0 && (!dst || !src))) return fail(PFGB_ERR_ARGUMENT, "invalid collection");
+  for (int i = 0; i < n; ++i) {
+    int rc = direction >= 0 ? pfgb_forward(P, dst[i], src[i], stream)
+                            : pfgb_backward(P, dst[i], src[i], stream, normalise);
+    if (rc) return rc;
+  }
+  return PFGB_OK;
+}
+
+}  // extern "C"

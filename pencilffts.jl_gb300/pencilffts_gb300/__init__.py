@@ -1,0 +1,17 @@
+"""GB300 (sm_103a) implementation of the PencilFFTs.jl transform path.
+
+The API mirrors the reference's ``PencilFFTPlan`` / ``Transforms`` interface at
+``proc_dims = (1, ..., 1)``; all transform arithmetic runs in the CUDA library
+``libpencilfft_gb300.so`` behind the C ABI of ``include/pencilfft_gb300.h``.
+"""
+from . import transforms as Transforms
+from ._lib import ArgumentError, LibraryError, load as load_library
+from .plans import (ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
+                    allocate_input, allocate_output, bmul_, gather, is_inplace,
+                    ldiv, ldiv_, mul_, plan_query, scale_factor)
+
+__all__ = [
+    "Transforms", "ArgumentError", "LibraryError", "load_library", "ManyPencilArray",
+    "Pencil", "PencilArray", "PencilFFTPlan", "Val", "allocate_input", "allocate_output",
+    "bmul_", "gather", "is_inplace", "ldiv", "ldiv_", "mul_", "plan_query", "scale_factor",
+]

@@ -1,0 +1,525 @@
+"""``PencilFFTPlan``, pencil arrays and the ``mul!``/``ldiv!``/``bmul!`` API.
+
+Host-side mirror of the reference's user API (``src/plans.jl``,
+``src/operations.jl``, ``src/allocate.jl``, ``src/multiarrays_r2c.jl``) at
+``proc_dims = (1, ..., 1)``.  Device memory comes from PyTorch; every transform
+runs in libpencilfft_gb300.so through its C ABI.
+
+Julia names ending in ``!`` are spelled with a trailing underscore:
+``mul_(dst, plan, src)`` is ``mul!(dst, plan, src)``; ``plan * u`` works as in
+Julia and ``ldiv(plan, uF)`` (or ``plan.ldiv(uF)``) is ``plan \\ uF``.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import ArgumentError, PlanDesc, PlanInfo
+from . import transforms as T
+
+_TORCH = None
+
+
+def _torch():
+    global _TORCH
+    if _TORCH is None:
+        import torch
+        _TORCH = torch
+    return _TORCH
+
+
+def _torch_dtype(dt: np.dtype):
+    torch = _torch()
+    return {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+            np.dtype(np.complex64): torch.complex64,
+            np.dtype(np.complex128): torch.complex128}[np.dtype(dt)]
+
+
+# ---------------------------------------------------------------------------
+# Pencils and arrays
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Pencil:
+    """Global logical sizes and memory order of one pencil configuration.
+
+    ``perm`` lists the logical dimensions (0-based) from fastest to slowest in
+    memory; extra dimensions always follow, slowest.  ``pitch0`` is the
+    allocated length of the fastest dimension (padded real views of in-place
+    r2c plans, reference src/multiarrays_r2c.jl:69-79).
+    """
+    dims: tuple
+    perm: tuple
+    extra_dims: tuple = ()
+    pitch0: int = 0
+
+    @property
+    def ndims(self):
+        return len(self.dims)
+
+    def memory_shape(self) -> tuple:
+        """C-order shape of the memory buffer (slowest first)."""
+        fast = [self.dims[d] for d in self.perm]
+        if self.pitch0:
+            fast[0] = self.pitch0
+        return tuple(reversed(self.extra_dims)) + tuple(reversed(fast))
+
+    def logical_permutation(self) -> tuple:
+        """Axes permutation taking the memory tensor to logical index order.
+
+        Memory axis i < K holds extra dimension K-1-i; memory axis K+q holds
+        logical dimension perm[N-1-q].
+        """
+        N, K = len(self.dims), len(self.extra_dims)
+        axis_to_logical = [N + (K - 1 - i) for i in range(K)]
+        axis_to_logical += [self.perm[N - 1 - q] for q in range(N)]
+        inv = [0] * (N + K)
+        for ax, lg in enumerate(axis_to_logical):
+            inv[lg] = ax
+        return tuple(inv)
+
+    def size_global(self, logical=True):
+        return self.dims if logical else tuple(self.dims[d] for d in self.perm)
+
+
+class PencilArray:
+    """A device array attached to a pencil (reference PencilArrays.PencilArray).
+
+    ``parent`` is the torch tensor in memory order (C-order shape
+    ``pencil.memory_shape()``); ``logical()`` is a view indexed like the
+    Julia array ``u[i1, ..., iN, e1, ...]``.
+    """
+
+    def __init__(self, pencil: Pencil, data, dtype):
+        self.pencil = pencil
+        self.data = data
+        self.dtype = np.dtype(dtype)
+
+    @property
+    def parent(self):
+        return self.data
+
+    def data_ptr(self) -> int:
+        return self.data.data_ptr()
+
+    def nbytes(self) -> int:
+        return self.data.numel() * self.data.element_size()
+
+    def logical(self):
+        v = self.data.permute(*self.pencil.logical_permutation())
+        if self.pencil.pitch0:
+            d0 = self.pencil.perm[0]
+            v = v.narrow(d0, 0, self.pencil.dims[d0])
+        return v
+
+    @property
+    def shape(self):
+        return tuple(self.pencil.dims) + tuple(self.pencil.extra_dims)
+
+    def size_global(self):
+        return self.shape
+
+    def copy_from_logical(self, arr):
+        """Fills the array from a logical numpy/torch array."""
+        torch = _torch()
+        src = torch.as_tensor(np.asarray(arr) if not isinstance(arr, torch.Tensor) else arr)
+        self.logical().copy_(src.to(self.data.device, dtype=self.data.dtype))
+        return self
+
+    def to_logical(self) -> np.ndarray:
+        """Host copy in logical index order (reference ``gather``)."""
+        return np.ascontiguousarray(self.logical().cpu().numpy())
+
+    def fill_(self, v):
+        self.data.fill_(v)
+        return self
+
+    def __repr__(self):
+        return f"PencilArray{{{self.dtype}}}(dims={self.shape}, perm={self.pencil.perm})"
+
+
+class ManyPencilArray:
+    """Several pencil views aliasing one buffer (reference PencilArrays.ManyPencilArray
+    and ``ManyPencilArrayRFFT!``, src/multiarrays_r2c.jl:26-79).  ``first()`` is
+    the input view, ``last()`` the output view of an in-place plan."""
+
+    def __init__(self, buffer, arrays: Sequence[PencilArray]):
+        self.buffer = buffer
+        self.arrays = tuple(arrays)
+
+    def first(self) -> PencilArray:
+        return self.arrays[0]
+
+    def last(self) -> PencilArray:
+        return self.arrays[-1]
+
+    def data_ptr(self) -> int:
+        return self.buffer.data_ptr()
+
+    def __repr__(self):
+        return f"ManyPencilArray({', '.join(repr(a) for a in self.arrays)})"
+
+
+def gather(A) -> np.ndarray:
+    """reference PencilArrays.gather at one process: the full logical array."""
+    return A.to_logical()
+
+
+# ---------------------------------------------------------------------------
+# Plan
+# ---------------------------------------------------------------------------
+def _expand(transforms, N):
+    if isinstance(transforms, T.AbstractTransform):
+        return T.expand_dims(transforms, N)
+    transforms = tuple(transforms)
+    if len(transforms) != N:
+        raise ArgumentError(f"expected {N} transforms, got {len(transforms)}")
+    return transforms
+
+
+def _descriptor(dims, transforms, real_type, permute_dims, extra_dims) -> PlanDesc:
+    N = len(dims)
+    if N < 1 or N > _lib.MAX_DIMS:
+        raise ArgumentError(f"number of dimensions must be in [1, {_lib.MAX_DIMS}]")
+    if len(extra_dims) > _lib.MAX_EXTRA:
+        raise ArgumentError("too many extra dimensions")
+    d = PlanDesc()
+    d.ndims = N
+    for n, (sz, tr) in enumerate(zip(dims, transforms)):
+        d.dims[n] = int(sz)
+        d.kind[n] = tr._abi_kind
+        d.inplace[n] = 1 if tr.inplace else 0
+        d.r2r_kind[n] = tr.kind if isinstance(tr, T.R2R) else 0
+        d.brfft_even[n] = 1 if (isinstance(tr, T.BRFFT) and tr.even_output) else 0
+    rt = np.dtype(real_type)
+    if rt not in (np.dtype(np.float32), np.dtype(np.float64)):
+        raise ArgumentError("real_type must be float32 or float64")
+    d.real_bytes = rt.itemsize
+    d.permute_dims = 1 if permute_dims else 0
+    d.n_extra = len(extra_dims)
+    for e, sz in enumerate(extra_dims):
+        d.extra_dims[e] = int(sz)
+    d.precision_mode = 0
+    d.autotune = 0
+    return d
+
+
+def plan_query(dims, transforms, real_type=np.float64, *, permute_dims=True, extra_dims=()):
+    """Host-only analysis of a plan through the C ABI (no GPU needed)."""
+    dims = tuple(int(x) for x in dims)
+    transforms = _expand(transforms, len(dims))
+    desc = _descriptor(dims, transforms, real_type, permute_dims, tuple(extra_dims))
+    info = PlanInfo()
+    L = _lib.load()
+    _lib.check(L.pfgb_plan_query(ctypes.byref(desc), ctypes.byref(info)), "pfgb_plan_query")
+    return info
+
+
+class PencilFFTPlan:
+    """N-dimensional FFT-based transform plan (reference ``PencilFFTPlan``).
+
+    ``PencilFFTPlan(dims_global, transforms, real_type=float64; permute_dims,
+    extra_dims)`` mirrors the reference constructor ``src/plans.jl:306-320``;
+    ``proc_dims`` must be all ones (one GPU, no MPI).  FFTW planning keywords
+    (``fftw_flags``, ``fftw_timelimit``) and ``transpose_method`` are accepted
+    and ignored, as the reference does for GPU arrays (src/plans.jl:325-332).
+    """
+
+    def __init__(self, dims_global, transforms, real_type=np.float64, *,
+                 proc_dims=None, permute_dims=True, extra_dims=(),
+                 fftw_flags=None, fftw_timelimit=None, transpose_method=None,
+                 timer=None, stream=None):
+        dims = tuple(int(x) for x in dims_global)
+        if proc_dims is not None and any(int(p) != 1 for p in proc_dims):
+            raise ArgumentError("this implementation runs on one GPU: proc_dims must be all ones")
+        if isinstance(permute_dims, bool) is False and permute_dims not in (0, 1):
+            raise ArgumentError("permute_dims must be a Bool")
+        self.transforms = _expand(transforms, len(dims))
+        if T.is_inplace(*self.transforms) is None:
+            raise ArgumentError(
+                f"cannot combine in-place and out-of-place transforms: {self.transforms}")
+        self.real_type = np.dtype(real_type)
+        self.permute_dims = bool(permute_dims)
+        self.extra_dims = tuple(int(e) for e in extra_dims)
+        self.timer = timer
+        self._stream = stream
+        desc = _descriptor(dims, self.transforms, self.real_type, self.permute_dims, self.extra_dims)
+        L = _lib.load()
+        handle = ctypes.c_void_p()
+        _lib.check(L.pfgb_plan_create(ctypes.byref(desc), ctypes.byref(handle)), "pfgb_plan_create")
+        self._handle = handle
+        self._L = L
+        info = PlanInfo()
+        _lib.check(L.pfgb_plan_info_get(handle, ctypes.byref(info)), "pfgb_plan_info_get")
+        self.info = info
+        N = len(dims)
+        self.ndims = N
+        self.size_global_in = dims
+        self.size_global_out = tuple(int(info.dims_out[n]) for n in range(N))
+        cdt = np.dtype(np.complex64) if self.real_type == np.float32 else np.dtype(np.complex128)
+        self._eltype_in = cdt if info.eltype_in_complex else self.real_type
+        self._eltype_out = cdt if info.eltype_out_complex else self.real_type
+        self._scale = float(info.scale_factor)
+        self._inplace = bool(info.inplace)
+        perm_out = tuple(int(info.perm_out[q]) for q in range(N))
+        natural = tuple(range(N))
+        pad = 0
+        if self._inplace and isinstance(self.transforms[0], T.RFFT):
+            pad = 2 * (dims[0] // 2 + 1)
+        self._pencil_in = Pencil(dims, natural, self.extra_dims, pad)
+        self._pencil_out = Pencil(self.size_global_out, perm_out, self.extra_dims)
+
+    # -- queries (reference plans.jl:338-361, 564-591) -------------------
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                self._L.pfgb_plan_destroy(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    def size(self):
+        return self.size_global_in
+
+    @property
+    def scale_factor(self) -> float:
+        return self._scale
+
+    def is_inplace(self) -> bool:
+        return self._inplace
+
+    def eltype_input(self):
+        return self._eltype_in
+
+    def eltype_output(self):
+        return self._eltype_out
+
+    def pencil_input(self) -> Pencil:
+        return self._pencil_in
+
+    def pencil_output(self) -> Pencil:
+        return self._pencil_out
+
+    def get_comm(self):
+        return None
+
+    def __repr__(self):
+        s = (f"Transforms: {self.transforms}\nInput type: {self._eltype_in}\n"
+             f"Global dimensions: {self.size_global_in} -> {self.size_global_out}")
+        if self.extra_dims:
+            s += f"\nExtra dimensions: {self.extra_dims}"
+        return s + "\nDevice: one GB300 (proc_dims all ones)"
+
+    # -- per-pass timing (reference: TimerOutputs sections) -----------------
+    def set_timing(self, on: bool = True):
+        _lib.check(self._L.pfgb_plan_set_timing(self._handle, 1 if on else 0), "pfgb_plan_set_timing")
+
+    def get_timing(self):
+        """Per-pass event timings recorded since the last call (synchronises)."""
+        buf = (_lib.PassTiming * 64)()
+        n = ctypes.c_int(0)
+        _lib.check(self._L.pfgb_plan_get_timing(self._handle, buf, 64, ctypes.byref(n)),
+                   "pfgb_plan_get_timing")
+        out = []
+        for i in range(min(n.value, 64)):
+            e = buf[i]
+            out.append(dict(direction=e.direction, pass_=e.pass_, axis=e.axis, op=e.op,
+                            launches=e.launches, total_ms=e.total_ms,
+                            bytes_per_launch=e.bytes_per_launch,
+                            kernel=e.kernel.decode()))
+        return out
+
+    # -- allocation (reference src/allocate.jl) ----------------------------
+    def _new_pencil_array(self, pencil: Pencil, dtype):
+        torch = _torch()
+        t = torch.empty(pencil.memory_shape(), dtype=_torch_dtype(dtype), device="cuda")
+        return PencilArray(pencil, t, dtype)
+
+    def _new_many(self):
+        torch = _torch()
+        nbytes = int(self.info.inplace_bytes)
+        buf = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        views = []
+        for pen, dt in ((self._pencil_in, self._eltype_in), (self._pencil_out, self._eltype_out)):
+            shape = pen.memory_shape()
+            n = int(np.prod(shape)) * np.dtype(dt).itemsize
+            t = buf[:n].view(_torch_dtype(dt)).view(shape)
+            views.append(PencilArray(pen, t, dt))
+        return ManyPencilArray(buf, views)
+
+    def _allocate(self, which):
+        if self._inplace:
+            return self._new_many()
+        if which == "in":
+            return self._new_pencil_array(self._pencil_in, self._eltype_in)
+        return self._new_pencil_array(self._pencil_out, self._eltype_out)
+
+    def allocate_input(self, *dims):
+        return _allocate_many(lambda: self._allocate("in"), dims)
+
+    def allocate_output(self, *dims):
+        return _allocate_many(lambda: self._allocate("out"), dims)
+
+    # -- execution ---------------------------------------------------------
+    def _stream_ptr(self):
+        if self._stream is not None:
+            return ctypes.c_void_p(int(self._stream))
+        torch = _torch()
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def _check_arrays(self, A_in, A_out):
+        """reference operations.jl:87-127.  ``A_in`` holds data of the plan's
+        input pencil and ``A_out`` of its output pencil (for a backward
+        transform, the destination and the source respectively)."""
+        s = "in-place" if self._inplace else "out-of-place"
+        if self._inplace:
+            if not (isinstance(A_in, ManyPencilArray) and isinstance(A_out, ManyPencilArray)):
+                raise ArgumentError(f"array types ({type(A_in).__name__}, {type(A_out).__name__}) "
+                                    f"incompatible with {s} plans")
+            if A_in is not A_out:
+                raise ArgumentError("input and output arrays for in-place plan must be the same")
+            pin, pout = A_in.first(), A_in.last()
+        else:
+            if not (isinstance(A_in, PencilArray) and isinstance(A_out, PencilArray)):
+                raise ArgumentError(f"array types ({type(A_in).__name__}, {type(A_out).__name__}) "
+                                    f"incompatible with {s} plans")
+            a0, a1 = A_in.data_ptr(), A_in.data_ptr() + A_in.nbytes()
+            b0, b1 = A_out.data_ptr(), A_out.data_ptr() + A_out.nbytes()
+            if a0 < b1 and b0 < a1:
+                raise ArgumentError("out-of-place plan applied to aliased data")
+            pin, pout = A_in, A_out
+        if pin.pencil != self._pencil_in or pin.dtype != self._eltype_in:
+            raise ArgumentError("unexpected dimensions of input data")
+        if pout.pencil != self._pencil_out or pout.dtype != self._eltype_out:
+            raise ArgumentError("unexpected dimensions of output data")
+
+    def _run(self, dst, src, forward: bool, normalise: bool):
+        L = self._L
+        stream = self._stream_ptr()
+        if forward:
+            self._check_arrays(src, dst)
+            rc = L.pfgb_forward(self._handle, ctypes.c_void_p(dst.data_ptr()),
+                                ctypes.c_void_p(src.data_ptr()), stream)
+            _lib.check(rc, "pfgb_forward")
+        else:
+            self._check_arrays(dst, src)
+            rc = L.pfgb_backward(self._handle, ctypes.c_void_p(dst.data_ptr()),
+                                 ctypes.c_void_p(src.data_ptr()), stream, 1 if normalise else 0)
+            _lib.check(rc, "pfgb_backward")
+        return dst
+
+    def _maybe_allocate(self, which, src):
+        """reference operations.jl:72-85."""
+        s = "in-place" if self._inplace else "out-of-place"
+        if self._inplace:
+            if not isinstance(src, ManyPencilArray):
+                raise ArgumentError(f"input array type {type(src).__name__} incompatible with {s} plans")
+            return src
+        if not isinstance(src, PencilArray):
+            raise ArgumentError(f"input array type {type(src).__name__} incompatible with {s} plans")
+        return self._allocate(which)
+
+    def __mul__(self, src):
+        """``plan * u`` (reference operations.jl:54-57); maps over collections."""
+        if _is_collection(src):
+            return type(src)(self * s for s in src) if isinstance(src, tuple) else [self * s for s in src]
+        dst = self._maybe_allocate("out", src)
+        return mul_(dst, self, src)
+
+    def ldiv(self, src):
+        """``plan \\ uF`` (reference operations.jl:59-62)."""
+        if _is_collection(src):
+            return type(src)(self.ldiv(s) for s in src) if isinstance(src, tuple) else [self.ldiv(s) for s in src]
+        dst = self._maybe_allocate("in", src)
+        return ldiv_(dst, self, src)
+
+
+def _is_collection(x):
+    return isinstance(x, (tuple, list))
+
+
+def _allocate_many(alloc, dims):
+    """reference allocate.jl:442-446: ``dims...`` -> nested lists, ``Val(N)`` -> tuple."""
+    if not dims:
+        return alloc()
+    if len(dims) == 1 and isinstance(dims[0], Val):
+        return tuple(alloc() for _ in range(dims[0].n))
+
+    def build(ds):
+        if len(ds) == 1:
+            return [alloc() for _ in range(ds[0])]
+        return [build(ds[1:]) for _ in range(ds[0])]
+    return build(tuple(int(d) for d in dims))
+
+
+class Val:
+    """Stand-in for Julia's ``Val(N)`` in ``allocate_input(plan, Val(3))``."""
+
+    def __init__(self, n):
+        self.n = int(n)
+
+
+def _flatten(x):
+    if _is_collection(x):
+        out = []
+        for e in x:
+            out.extend(_flatten(e))
+        return out
+    return [x]
+
+
+def _check_compatible(a, b):
+    """reference operations.jl:130-137."""
+    if len(a) != len(b):
+        raise ArgumentError(f"collections have different lengths: {len(a)} ≠ {len(b)}")
+
+
+def _apply(dst, plan, src, forward, normalise):
+    if _is_collection(dst) or _is_collection(src):
+        if not (_is_collection(dst) and _is_collection(src)):
+            raise ArgumentError("collections and single arrays cannot be mixed")
+        _check_compatible(dst, src)
+        for d, s in zip(dst, src):
+            _apply(d, plan, s, forward, normalise)
+        return dst
+    return plan._run(dst, src, forward, normalise)
+
+
+def mul_(dst, plan: PencilFFTPlan, src):
+    """``mul!(dst, plan, src)``: forward transform (reference operations.jl:24-31)."""
+    return _apply(dst, plan, src, True, False)
+
+
+def ldiv_(dst, plan: PencilFFTPlan, src):
+    """``ldiv!(dst, plan, src)``: normalised backward transform (operations.jl:44-52)."""
+    return _apply(dst, plan, src, False, True)
+
+
+def bmul_(dst, plan: PencilFFTPlan, src):
+    """``bmul!(dst, plan, src)``: unnormalised backward transform (operations.jl:34-41)."""
+    return _apply(dst, plan, src, False, False)
+
+
+def ldiv(plan: PencilFFTPlan, src):
+    """``plan \\ src``."""
+    return plan.ldiv(src)
+
+
+def allocate_input(plan: PencilFFTPlan, *dims):
+    return plan.allocate_input(*dims)
+
+
+def allocate_output(plan: PencilFFTPlan, *dims):
+    return plan.allocate_output(*dims)
+
+
+def scale_factor(plan: PencilFFTPlan) -> float:
+    return plan.scale_factor
+
+
+def is_inplace(plan: PencilFFTPlan) -> bool:
+    return plan.is_inplace()

@@ -1,0 +1,52 @@
+"""The C ABI library loads and exports every symbol include/pencilfft_gb300.h
+declares (no compute call; CPU only)."""
+import ctypes
+import os
+import re
+
+import pencilffts_gb300 as P
+from pencilffts_gb300 import _lib
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(REPO, "include")):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(REPO, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(pfgb_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_symbols_exported():
+    L = P.load_library()
+    names = declared_symbols()
+    assert "pfgb_forward" in names and "pfgb_plan_create" in names
+    for n in names:
+        assert hasattr(L, n), f"{n} declared in include/ but not exported"
+    # the ctypes table covers every declared entry point
+    assert names <= set(_lib.SIGNATURES), names - set(_lib.SIGNATURES)
+
+
+def test_struct_layouts_match_header():
+    # pfgb_plan_desc: int32 + 8 int64 + 4*8 int32 + 3 int32 + 4 int64 + 2 int32
+    assert ctypes.sizeof(_lib.PlanDesc) == 4 + 4 + 64 + 4 * 32 + 12 + 4 + 32 + 8
+    assert ctypes.alignment(_lib.PlanDesc) == 8
+
+
+def test_version_and_error_buffer():
+    L = P.load_library()
+    assert b"sm_103a" in L.pfgb_version()
+    buf = ctypes.create_string_buffer(8)
+    L.pfgb_last_error(buf, len(buf))  # callable without a device
+
+
+def test_null_arguments_rejected_without_device():
+    L = P.load_library()
+    assert L.pfgb_plan_create(None, None) == _lib.ERR_ARGUMENT
+    assert L.pfgb_forward(None, None, None, None) == _lib.ERR_ARGUMENT
+    assert L.pfgb_plan_destroy(None) == _lib.OK
