@@ -38,6 +38,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--dims", default="512,512,512")
     ap.add_argument("--real", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--precision", default="default", choices=["default", "native"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-s", type=float, default=20.0,
@@ -176,7 +177,7 @@ def run_gpu(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    plan = P.PencilFFTPlan(dims, T.RFFT(), real)
+    plan = P.PencilFFTPlan(dims, T.RFFT(), real, precision=args.precision)
     u = plan.allocate_input()
     v = plan.allocate_output()
     g = torch.Generator(device=dev)
@@ -294,6 +295,7 @@ def run_gpu(args, rank, world, local_rank):
                                "permute_dims=true, out-of-place",
                    "dims": list(dims), "transforms": "RFFT (RFFT, FFT, FFT)",
                    "l2": "inputs larger than L2 (1.07 GB arrays)",
+                   "precision": args.precision,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "hbm_gbs": alg_rt / (ms_step * 1e-3) / 1e9 * world,
         "gflops": 2 * 2.5 * np.prod(dims) * np.log2(np.prod(dims)) / (ms_step * 1e-3) / 1e9 * world,

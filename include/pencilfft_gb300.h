@@ -75,9 +75,18 @@ typedef struct pfgb_plan_desc {
   int32_t permute_dims;               /* 1 = Val(true) (default), 0 = Val(false) */
   int32_t n_extra;                    /* number of extra_dims */
   int64_t extra_dims[PFGB_MAX_EXTRA];
-  int32_t precision_mode;             /* 0 = plain arithmetic of real_bytes */
+  int32_t precision_mode;             /* PFGB_PRECISION_* */
   int32_t autotune;                   /* 0 = off */
 } pfgb_plan_desc;
+
+/* Arithmetic of the transform kernels.
+ *   DEFAULT: Float32 plans compute in FP32; Float64 plans compute power-of-two
+ *            c2c/r2c/c2r lines in double-float (two FP32 values, 48-bit
+ *            significand, on the FP32 pipes) and every other line in native
+ *            FP64.  Both meet a relative L2 error of 1e-13.
+ *   NATIVE:  Float64 plans compute every line in native FP64 (GB300's FP64
+ *            rate is about 1/70 of its FP32 rate). */
+enum { PFGB_PRECISION_DEFAULT = 0, PFGB_PRECISION_NATIVE = 1 };
 
 typedef struct pfgb_plan pfgb_plan;
 

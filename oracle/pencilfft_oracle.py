@@ -347,9 +347,11 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     """Relative L2 error ``|a - b| / |b|`` computed in long double."""
     a = np.asarray(a).astype(np.clongdouble)
     b = np.asarray(b).astype(np.clongdouble)
-    den = math.sqrt(float(np.sum(np.abs(b) ** 2)))
-    num = math.sqrt(float(np.sum(np.abs(a - b) ** 2)))
-    return num / den if den > 0 else num
+    den = np.sum(np.abs(b) ** 2)
+    num = np.sum(np.abs(a - b) ** 2)
+    if den > 0:
+        return math.sqrt(float(num / den))
+    return math.sqrt(float(num))
 
 
 def max_abs(a, b) -> float:

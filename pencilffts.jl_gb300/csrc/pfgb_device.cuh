@@ -128,36 +128,43 @@ __device__ __forceinline__ void dft4(Cx<R>& x0, Cx<R>& x1, Cx<R>& x2, Cx<R>& x3)
   x3 = t1 - t3;
 }
 
-// exp(SIGN i pi m / 8) for the compile-time exponent m in [0, 16).
+// x * exp(SIGN i pi m / 8) for the compile-time exponent m in [0, 16).
 template <int SIGN, int m, typename R>
 __device__ __forceinline__ Cx<R> w16mul(Cx<R> x) {
   constexpr int mm = m & 15;
-  const R c1 = R(0.92387953251128675613);  // cos(pi/8)
-  const R s1 = R(0.38268343236508977173);  // sin(pi/8)
-  const R h = R(0.70710678118654752440);   // cos(pi/4)
-  const R sg = SIGN < 0 ? R(-1) : R(1);
-  if (mm == 0) return x;
-  if (mm == 4) return mul_w4<SIGN>(x);
-  if (mm == 8) return -x;
-  if (mm == 12) return mul_w4<-SIGN>(x);
-  // general: angle = SIGN * pi * mm / 8
-  R c, s;
-  switch (mm) {
-    case 1: c = c1; s = s1; break;
-    case 2: c = h; s = h; break;
-    case 3: c = s1; s = c1; break;
-    case 5: c = -s1; s = c1; break;
-    case 6: c = -h; s = h; break;
-    case 7: c = -c1; s = s1; break;
-    case 9: c = -c1; s = -s1; break;
-    case 10: c = -h; s = -h; break;
-    case 11: c = -s1; s = -c1; break;
-    case 13: c = s1; s = -c1; break;
-    case 14: c = h; s = -h; break;
-    default: c = c1; s = -s1; break;  // 15
+  if constexpr (mm == 0) {
+    return x;
+  } else if constexpr (mm == 4) {
+    return mul_w4<SIGN>(x);
+  } else if constexpr (mm == 8) {
+    return -x;
+  } else if constexpr (mm == 12) {
+    return mul_w4<-SIGN>(x);
+  } else if constexpr ((mm & 3) == 2) {
+    // odd multiples of pi/4: (c, s) = h (+-1, +-1), h = cos(pi/4)
+    const R h = R(0.70710678118654752440);
+    constexpr int cs = (mm == 2 || mm == 14) ? 1 : -1;                      // sign of cos
+    constexpr int ss = ((mm == 2 || mm == 6) ? 1 : -1) * (SIGN < 0 ? -1 : 1);  // sign of sin
+    // (re c - im s, re s + im c) with |c| = |s| = h
+    R a = (cs > 0) ? x.re : -x.re;
+    R b = (ss > 0) ? x.im : -x.im;
+    R c2 = (ss > 0) ? x.re : -x.re;
+    R d2 = (cs > 0) ? x.im : -x.im;
+    return mk((a - b) * h, (c2 + d2) * h);
+  } else {
+    const R c1 = R(0.92387953251128675613);  // cos(pi/8)
+    const R s1 = R(0.38268343236508977173);  // sin(pi/8)
+    // angle pi mm / 8 for the odd mm: cos and sin as +-c1 / +-s1
+    constexpr bool swap = (mm == 3 || mm == 5 || mm == 11 || mm == 13);
+    constexpr int cs = (mm == 1 || mm == 3 || mm == 13 || mm == 15) ? 1 : -1;
+    constexpr int ss0 = (mm < 8) ? 1 : -1;
+    constexpr int ss = ss0 * (SIGN < 0 ? -1 : 1);
+    R c = swap ? s1 : c1;
+    R s = swap ? c1 : s1;
+    if constexpr (cs < 0) c = -c;
+    if constexpr (ss < 0) s = -s;
+    return mk(x.re * c - x.im * s, x.re * s + x.im * c);
   }
-  s = sg * s;
-  return mk(x.re * c - x.im * s, x.re * s + x.im * c);
 }
 
 template <int SIGN, typename R>

@@ -22,6 +22,7 @@
 
 #include "pencilfft_gb300.h"
 #include "pfgb_device.cuh"
+#include "pfgb_fast.cuh"
 
 namespace pfgb {
 
@@ -100,6 +101,10 @@ struct Pass {
   const void* chirp = nullptr;
   const void* bfilt = nullptr;
   const void* r2rtw = nullptr;
+  // register Stockham kernel for power-of-two lines (fast_pass)
+  bool fast = false;
+  int logm = 0;
+  const void* ftw = nullptr;  // its twiddle table (float or dd entries)
   // launch geometry
   int lines = 1, clines = 1, bpl = 1, lp = 0, threads = 0;
   size_t smem = 0;
@@ -118,6 +123,7 @@ struct pfgb_plan {
   pfgb_plan_desc desc;
   int N = 0, K = 0, D = 0;
   int rb = 8;  // real bytes
+  int precision = 0;  // PFGB_PRECISION_*
   bool inplace = false;
   bool permute = true;
   int64_t dims_in[pfgb::kMaxD] = {}, dims_out[pfgb::kMaxD] = {};
@@ -243,6 +249,43 @@ static int upload_table(pfgb_plan* P, const std::string& key,
   return PFGB_OK;
 }
 
+// Twiddles of the fast kernel: float (re, im) for Float32 plans, dd
+// (re.hi, re.lo, im.hi, im.lo) for Float64 plans.
+static int upload_fast_table(pfgb_plan* P, int M, const void** out) {
+  if (P->query_only) {
+    *out = nullptr;
+    return PFGB_OK;
+  }
+  const std::string key = (P->rb == 8 ? "ftwdd" : "ftwf") + std::to_string(M);
+  auto it = P->tables.find(key);
+  if (it != P->tables.end()) {
+    *out = it->second;
+    return PFGB_OK;
+  }
+  std::vector<float> h;
+  h.reserve((size_t)M * 4);
+  for (int m = 0; m < M; ++m) {
+    const std::complex<ld> w = expi_pi(2 * (int64_t)m, M);
+    if (P->rb == 8) {
+      for (ld c : {w.real(), w.imag()}) {
+        const float hi = (float)c;
+        const float lo = (float)(c - (ld)hi);
+        h.push_back(hi);
+        h.push_back(lo);
+      }
+    } else {
+      h.push_back((float)w.real());
+      h.push_back((float)w.imag());
+    }
+  }
+  void* d = nullptr;
+  PFGB_CUDA(cudaMalloc(&d, h.size() * sizeof(float)));
+  PFGB_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  P->tables[key] = d;
+  *out = d;
+  return PFGB_OK;
+}
+
 // Radix plan for a DFT length: returns false if a prime factor > 13 remains.
 static bool factor_radices(int n, std::vector<int>& rad) {
   rad.clear();
@@ -355,6 +398,22 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   }
   int rc = prepare_core(P, ps, M);
   if (rc) return rc;
+  // power-of-two c2c / r2c / c2r lines take the register Stockham kernel; on
+  // Float64 plans it computes in dd unless native FP64 was requested
+  if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && ps.L == 0 && M >= 8 &&
+      M <= 4096 && (M & (M - 1)) == 0 && !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+    ps.fast = true;
+    ps.logm = 0;
+    while ((1 << ps.logm) < M) ++ps.logm;
+    rc = upload_fast_table(P, M, &ps.ftw);
+    if (rc) return rc;
+    const bool packed = ps.op != OP_C2C;
+    ps.clines = fast_tw(ps.logm);
+    ps.lines = packed ? 2 * ps.clines : ps.clines;
+    ps.threads = fast_threads();
+    ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm) : fast_smem<float>(ps.logm);
+    return PFGB_OK;
+  }
   const int Lc = ps.L > 0 ? ps.L : ps.M;
   int rmin = 64;
   for (int i = 0; i < ps.nst; ++i) rmin = std::min(rmin, ps.rad[i]);
@@ -455,6 +514,40 @@ static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* o
   return PFGB_OK;
 }
 
+static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, void* out,
+                          bool scale_on, FastArgs& F, int64_t& grid) {
+  PassArgs A;
+  int rc = make_args(P, ps, in, out, scale_on, A, grid);
+  if (rc) return rc;
+  std::memset(&F, 0, sizeof(F));
+  F.in = in;
+  F.out = out;
+  F.tw = ps.ftw;
+  F.op = ps.op;
+  F.n_in = A.n_in;
+  F.n_out = A.n_out;
+  F.lmap_tile = A.in_tfast;
+  F.out_tfast = A.out_tfast;
+  F.store_direct = A.in_tfast ? A.out_tfast : (A.out_sa == 1 ? 1 : 0);
+  F.scale_on = scale_on ? 1 : 0;
+  const ld sc = 1.0L / (ld)P->scale;
+  F.scale_h = (float)sc;
+  F.scale_l = (float)(sc - (ld)F.scale_h);
+  F.nouter = A.nouter;
+  F.nt = A.nt;
+  F.ntiles = A.ntiles;
+  F.in_sa = A.in_sa;
+  F.in_st = A.in_st;
+  F.out_sa = A.out_sa;
+  F.out_st = A.out_st;
+  for (int d = 0; d < A.nouter; ++d) {
+    F.osz[d] = A.osz[d];
+    F.in_so[d] = A.in_so[d];
+    F.out_so[d] = A.out_so[d];
+  }
+  return PFGB_OK;
+}
+
 static int make_copy_args(const Pass& ps, const void* in, void* out, CopyArgs& C) {
   std::memset(&C, 0, sizeof(C));
   C.in = in;
@@ -477,6 +570,8 @@ static int make_copy_args(const Pass& ps, const void* in, void* out, CopyArgs& C
 int launch_pass(int real_bytes, const PassArgs& A, int64_t grid, int threads, size_t smem,
                 cudaStream_t s);
 int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
+int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Schedule: build the passes of one direction and assign buffers.
@@ -731,6 +826,14 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       make_copy_args(ps, in, out, C);
       int rc = launch_copy(ps.lout.elt, C, s);
       if (rc) return rc;
+    } else if (ps.fast) {
+      FastArgs F;
+      int64_t grid = 0;
+      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid);
+      if (rc) return rc;
+      rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, s)
+                      : launch_fast_f32(ps.logm, ps.sign, F, grid, s);
+      if (rc) return rc;
     } else {
       PassArgs A;
       int64_t grid = 0;
@@ -779,7 +882,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
     return fail(PFGB_ERR_ARGUMENT, "too many extra_dims");
   if (d.real_bytes != 4 && d.real_bytes != 8)
     return fail(PFGB_ERR_ARGUMENT, "real type must be Float32 (4) or Float64 (8)");
-  if (d.precision_mode != 0)
+  if (d.precision_mode != PFGB_PRECISION_DEFAULT && d.precision_mode != PFGB_PRECISION_NATIVE)
     return fail(PFGB_ERR_UNSUPPORTED, "precision mode not available in this build");
   for (int n = 0; n < d.ndims; ++n) {
     if (d.dims[n] < 1) return fail(PFGB_ERR_ARGUMENT, "dimensions must be positive");
@@ -802,6 +905,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   P->K = d.n_extra;
   P->D = P->N + P->K;
   P->rb = d.real_bytes;
+  P->precision = d.precision_mode;
   P->inplace = d.inplace[0] != 0;
   P->permute = d.permute_dims != 0;
   if (!query_only) cudaGetDevice(&P->device);
@@ -940,7 +1044,9 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     e.axis = ps.axis;
     e.op = ps.pk == PK_COPY ? -1 : ps.op;
     e.bytes_per_launch = ps.lin.bytes() + ps.lout.bytes();
-    const char* kname = ps.pk == PK_COPY ? "copy_kernel" : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
+    const char* kname = ps.pk == PK_COPY ? "copy_kernel"
+                        : ps.fast ? (P->rb == 8 ? "fast_pass<dd>" : "fast_pass<float>")
+                                  : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);
     acc.push_back(e);
     return acc.back();

@@ -180,7 +180,10 @@ def _expand(transforms, N):
     return transforms
 
 
-def _descriptor(dims, transforms, real_type, permute_dims, extra_dims) -> PlanDesc:
+PRECISION = {"default": 0, "native": 1}
+
+
+def _descriptor(dims, transforms, real_type, permute_dims, extra_dims, precision="default") -> PlanDesc:
     N = len(dims)
     if N < 1 or N > _lib.MAX_DIMS:
         raise ArgumentError(f"number of dimensions must be in [1, {_lib.MAX_DIMS}]")
@@ -202,16 +205,19 @@ def _descriptor(dims, transforms, real_type, permute_dims, extra_dims) -> PlanDe
     d.n_extra = len(extra_dims)
     for e, sz in enumerate(extra_dims):
         d.extra_dims[e] = int(sz)
-    d.precision_mode = 0
+    if precision not in PRECISION:
+        raise ArgumentError(f"precision must be one of {tuple(PRECISION)}")
+    d.precision_mode = PRECISION[precision]
     d.autotune = 0
     return d
 
 
-def plan_query(dims, transforms, real_type=np.float64, *, permute_dims=True, extra_dims=()):
+def plan_query(dims, transforms, real_type=np.float64, *, permute_dims=True, extra_dims=(),
+               precision="default"):
     """Host-only analysis of a plan through the C ABI (no GPU needed)."""
     dims = tuple(int(x) for x in dims)
     transforms = _expand(transforms, len(dims))
-    desc = _descriptor(dims, transforms, real_type, permute_dims, tuple(extra_dims))
+    desc = _descriptor(dims, transforms, real_type, permute_dims, tuple(extra_dims), precision)
     info = PlanInfo()
     L = _lib.load()
     _lib.check(L.pfgb_plan_query(ctypes.byref(desc), ctypes.byref(info)), "pfgb_plan_query")
@@ -223,7 +229,10 @@ class PencilFFTPlan:
 
     ``PencilFFTPlan(dims_global, transforms, real_type=float64; permute_dims,
     extra_dims)`` mirrors the reference constructor ``src/plans.jl:306-320``;
-    ``proc_dims`` must be all ones (one GPU, no MPI).  FFTW planning keywords
+    ``proc_dims`` must be all ones (one GPU, no MPI).  ``precision`` selects
+    the kernel arithmetic of Float64 plans: "default" (double-float on the
+    FP32 pipes for power-of-two lines, FP64 elsewhere) or "native" (FP64
+    everywhere).  FFTW planning keywords
     (``fftw_flags``, ``fftw_timelimit``) and ``transpose_method`` are accepted
     and ignored, as the reference does for GPU arrays (src/plans.jl:325-332).
     """
@@ -231,7 +240,7 @@ class PencilFFTPlan:
     def __init__(self, dims_global, transforms, real_type=np.float64, *,
                  proc_dims=None, permute_dims=True, extra_dims=(),
                  fftw_flags=None, fftw_timelimit=None, transpose_method=None,
-                 timer=None, stream=None):
+                 timer=None, stream=None, precision="default"):
         dims = tuple(int(x) for x in dims_global)
         if proc_dims is not None and any(int(p) != 1 for p in proc_dims):
             raise ArgumentError("this implementation runs on one GPU: proc_dims must be all ones")
@@ -246,7 +255,9 @@ class PencilFFTPlan:
         self.extra_dims = tuple(int(e) for e in extra_dims)
         self.timer = timer
         self._stream = stream
-        desc = _descriptor(dims, self.transforms, self.real_type, self.permute_dims, self.extra_dims)
+        self.precision = precision
+        desc = _descriptor(dims, self.transforms, self.real_type, self.permute_dims, self.extra_dims,
+                           precision)
         L = _lib.load()
         handle = ctypes.c_void_p()
         _lib.check(L.pfgb_plan_create(ctypes.byref(desc), ctypes.byref(handle)), "pfgb_plan_create")

@@ -101,6 +101,38 @@ def test_small_and_unit_sizes(cuda, dims):
         check_plan(plan)
 
 
+@pytest.mark.parametrize("precision", ["default", "native"])
+@pytest.mark.parametrize("dims", [(16, 12, 6), (64, 32, 16), (8, 4096), (4096, 3), (512, 8, 2)])
+@pytest.mark.parametrize("tr", [T.RFFT(), T.FFT(), T.BFFT(), T.RFFT_(), T.FFT_()], ids=repr)
+def test_pow2_fast_path(cuda, dims, tr, precision):
+    """Power-of-two lines (register Stockham kernel), both Float64 arithmetics."""
+    plan = P.PencilFFTPlan(dims, tr, F64, precision=precision)
+    check_plan(plan)
+    if precision == "default":
+        check_plan(P.PencilFFTPlan(dims, tr, F32))
+
+
+@pytest.mark.parametrize("permute", [True, False])
+@pytest.mark.parametrize("edims", [(), (2,)])
+def test_fast_path_layouts(cuda, permute, edims):
+    for tr in (T.RFFT(), T.FFT(), T.BRFFT((32, 16, 64))):
+        check_plan(P.PencilFFTPlan((32, 16, 33) if isinstance(tr, T.BRFFT) else (32, 16, 64), tr, F64,
+                                   permute_dims=permute, extra_dims=edims))
+
+
+def test_dd_wide_dynamic_range(cuda):
+    """Float64 data far outside the float exponent range keeps full accuracy."""
+    plan = P.PencilFFTPlan((64, 32, 16), T.RFFT(), F64)
+    orc = oracle_plan(plan)
+    rng = np.random.default_rng(5)
+    for scale in (1e-200, 1e250):
+        x = rng.standard_normal((64, 32, 16)) * scale
+        A = input_array(plan, x)
+        B = plan * A
+        assert rel(B.to_logical(), orc.forward(x)) <= 1e-13
+        assert rel(plan.ldiv(B).to_logical(), x) <= 1e-13
+
+
 @pytest.mark.parametrize("n", [7, 11, 13, 17, 23, 41, 53, 97, 191, 384, 1000, 1024, 2048])
 @pytest.mark.parametrize("real", [F64, F32])
 def test_1d_lengths(cuda, n, real):
