@@ -34,6 +34,12 @@ struct FastArgs {
   int out_tfast;     // tile dimension contiguous in the output (smem store loop)
   int scale_on;
   float scale_h, scale_l;  // ldiv! normalisation as hi + lo
+  // Float64 (dd) passes: the input / output of a pass between two dd passes is
+  // kept in dd form (re.hi, re.lo, im.hi, im.lo floats), scaled by the run's
+  // power of two 2^(1023 - *emax) where *emax is the largest biased exponent of
+  // the run's double input (computed by emax_kernel before the run).
+  int in_dd, out_dd;
+  const int* emax_ptr;
   int nouter;
   int64_t nt, ntiles;
   int64_t in_sa, in_st, out_sa, out_st;
@@ -160,6 +166,18 @@ __device__ __forceinline__ typename FastIO<R>::MR outr(R x, int emax) {
   else return x;
 }
 
+// dd form of a complex value in memory: (re.hi, re.lo, im.hi, im.lo)
+template <typename R>
+__device__ __forceinline__ Cx<R> ld_dd4(float4 q) {
+  if constexpr (std::is_same<R, dd>::value) return mk(dd(q.x, q.y), dd(q.z, q.w));
+  else return mk(q.x, q.z);
+}
+template <typename R>
+__device__ __forceinline__ float4 st_dd4(Cx<R> y) {
+  if constexpr (std::is_same<R, dd>::value) return make_float4(y.re.h, y.re.l, y.im.h, y.im.l);
+  else return make_float4(y.re, 0.f, y.im, 0.f);
+}
+
 template <typename R>
 __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
   if (!a.scale_on) return y;
@@ -171,8 +189,18 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
   }
 }
 
+#ifndef PFGB_FAST_F32_MINBLOCKS
+#define PFGB_FAST_F32_MINBLOCKS 2
+#endif
+// float tiles fit two CTAs per SM at 64 registers per thread; dd needs more
+// registers and runs one 512-thread CTA per SM.
+template <typename R>
+__host__ __device__ constexpr int fast_min_blocks() {
+  return std::is_same<R, float>::value ? PFGB_FAST_F32_MINBLOCKS : 1;
+}
+
 template <typename R, int LOGM, int SIGN>
-__global__ void __launch_bounds__(512, 1) fast_pass(const FastArgs a) {
+__global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const FastArgs a) {
   using IO = FastIO<R>;
   using MR = typename IO::MR;
   using MC = typename IO::MC;
@@ -181,7 +209,6 @@ __global__ void __launch_bounds__(512, 1) fast_pass(const FastArgs a) {
   constexpr int TW = fast_tw(LOGM);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
-  __shared__ int s_red[32];
 
   const int tid = threadIdx.x;
   int p, b;
@@ -206,74 +233,57 @@ __global__ void __launch_bounds__(512, 1) fast_pass(const FastArgs a) {
   // ---- load: v[r] = line p, element b + r T (stage-1 Stockham inputs) ----
   Cx<R> v[8];
   int emax = 0;
+  if constexpr (IO::kDD) emax = *a.emax_ptr;
   if (a.op == OP_C2C) {
-    const MC* in = reinterpret_cast<const MC*>(a.in) + ioff + (int64_t)p * a.in_st;
-    MC raw[8];
+    if (IO::kDD && a.in_dd) {
+      const float4* in = reinterpret_cast<const float4*>(a.in) + ioff + (int64_t)p * a.in_st;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      raw[r] = p < nvalid ? in[(int64_t)(b + r * T) * a.in_sa] : MC{0, 0};
-      if constexpr (IO::kDD) emax = max(emax, max(dexp_bits(raw[r].x), dexp_bits(raw[r].y)));
-    }
-    if constexpr (IO::kDD) {
-      emax = __reduce_max_sync(0xffffffffu, emax);
-      if ((tid & 31) == 0) s_red[tid >> 5] = emax;
-      __syncthreads();
-      emax = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) emax = max(emax, s_red[w]);
-    }
+      for (int r = 0; r < 8; ++r) {
+        const float4 q = p < nvalid ? in[(int64_t)(b + r * T) * a.in_sa] : make_float4(0.f, 0.f, 0.f, 0.f);
+        v[r] = ld_dd4<R>(q);
+      }
+    } else {
+      const MC* in = reinterpret_cast<const MC*>(a.in) + ioff + (int64_t)p * a.in_st;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
+      for (int r = 0; r < 8; ++r) {
+        const MC raw = p < nvalid ? in[(int64_t)(b + r * T) * a.in_sa] : MC{0, 0};
+        v[r] = mk(mkr<R>(raw.x, emax), mkr<R>(raw.y, emax));
+      }
+    }
   } else if (a.op == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(a.in) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
-    MR ra[8], rb[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int64_t off = (int64_t)(b + r * T) * a.in_sa;
-      ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : MR(0);
-      rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : MR(0);
-      if constexpr (IO::kDD) emax = max(emax, max(dexp_bits(ra[r]), dexp_bits(rb[r])));
+      const MR ra = i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : MR(0);
+      const MR rb = i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : MR(0);
+      v[r] = mk(mkr<R>(ra, emax), mkr<R>(rb, emax));
     }
-    if constexpr (IO::kDD) {
-      emax = __reduce_max_sync(0xffffffffu, emax);
-      if ((tid & 31) == 0) s_red[tid >> 5] = emax;
-      __syncthreads();
-      emax = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) emax = max(emax, s_red[w]);
-    }
-#pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
   } else {  // OP_C2R: Hermitian extension of two half spectra, n = M, m = n_in
-    const MC* in = reinterpret_cast<const MC*>(a.in) + ioff;
     const int m = a.n_in;
     const int i0 = 2 * p, i1 = 2 * p + 1;
-    MC ra[8], rb[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int pos = b + r * T;
       const int k = pos < m ? pos : M - pos;
       const int64_t off = (int64_t)k * a.in_sa;
-      ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : MC{0, 0};
-      rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : MC{0, 0};
-      if (k == 0 || 2 * k == M) { ra[r].y = 0; rb[r].y = 0; }
-      if constexpr (IO::kDD)
-        emax = max(emax, max(max(dexp_bits(ra[r].x), dexp_bits(ra[r].y)),
-                             max(dexp_bits(rb[r].x), dexp_bits(rb[r].y))));
-    }
-    if constexpr (IO::kDD) {
-      emax = __reduce_max_sync(0xffffffffu, emax);
-      if ((tid & 31) == 0) s_red[tid >> 5] = emax;
-      __syncthreads();
-      emax = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) emax = max(emax, s_red[w]);
-    }
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int pos = b + r * T;
-      const R Ar = mkr<R>(ra[r].x, emax), Ai = mkr<R>(ra[r].y, emax);
-      const R Br = mkr<R>(rb[r].x, emax), Bi = mkr<R>(rb[r].y, emax);
+      Cx<R> A, B;
+      if (IO::kDD && a.in_dd) {
+        const float4* in = reinterpret_cast<const float4*>(a.in) + ioff;
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        A = ld_dd4<R>(i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : z4);
+        B = ld_dd4<R>(i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : z4);
+      } else {
+        const MC* in = reinterpret_cast<const MC*>(a.in) + ioff;
+        const MC ra = i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : MC{0, 0};
+        const MC rb = i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : MC{0, 0};
+        A = mk(mkr<R>(ra.x, emax), mkr<R>(ra.y, emax));
+        B = mk(mkr<R>(rb.x, emax), mkr<R>(rb.y, emax));
+      }
+      if (k == 0 || 2 * k == M) { A.im = R(0); B.im = R(0); }
       // pos < m: A + iB ; else conj(A) + i conj(B)
-      v[r] = pos < m ? mk(Ar - Bi, Ai + Br) : mk(Ar + Bi, Br - Ai);
+      v[r] = pos < m ? mk(A.re - B.im, A.im + B.re) : mk(A.re + B.im, B.re - A.im);
     }
   }
 
@@ -284,14 +294,20 @@ __global__ void __launch_bounds__(512, 1) fast_pass(const FastArgs a) {
   if (a.store_direct && a.op != OP_R2C) {
     if (a.op == OP_C2C) {
       if (p < nvalid) {
-        MC* out = reinterpret_cast<MC*>(a.out) + ooff + (int64_t)p * a.out_st;
+        if (IO::kDD && a.out_dd) {
+          float4* out = reinterpret_cast<float4*>(a.out) + ooff + (int64_t)p * a.out_st;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-          const Cx<R> y = apply_scale(v[r], a);
-          MC o;
-          o.x = outr<R>(y.re, emax);
-          o.y = outr<R>(y.im, emax);
-          out[(int64_t)(b + r * T) * a.out_sa] = o;
+          for (int r = 0; r < 8; ++r) out[(int64_t)(b + r * T) * a.out_sa] = st_dd4(apply_scale(v[r], a));
+        } else {
+          MC* out = reinterpret_cast<MC*>(a.out) + ooff + (int64_t)p * a.out_st;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const Cx<R> y = apply_scale(v[r], a);
+            MC o;
+            o.x = outr<R>(y.re, emax);
+            o.y = outr<R>(y.im, emax);
+            out[(int64_t)(b + r * T) * a.out_sa] = o;
+          }
         }
       }
     } else {  // C2R, real outputs of lines 2p and 2p+1
@@ -321,10 +337,14 @@ __global__ void __launch_bounds__(512, 1) fast_pass(const FastArgs a) {
       if (a.out_tfast) { i = e % TW; k = e / TW; } else { k = e % M; i = e / M; }
       if (i >= nvalid) continue;
       const Cx<R> y = apply_scale(z[sidx<LOGM>(i, k)], a);
-      MC o;
-      o.x = outr<R>(y.re, emax);
-      o.y = outr<R>(y.im, emax);
-      out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = o;
+      if (IO::kDD && a.out_dd) {
+        reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
+      } else {
+        MC o;
+        o.x = outr<R>(y.re, emax);
+        o.y = outr<R>(y.im, emax);
+        out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = o;
+      }
     }
   } else if (a.op == OP_R2C) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
@@ -340,17 +360,23 @@ __global__ void __launch_bounds__(512, 1) fast_pass(const FastArgs a) {
       B = apply_scale(mk(half(B.re), half(B.im)), a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
-      if (i0 < nvalid) {
-        MC o;
-        o.x = outr<R>(A.re, emax);
-        o.y = outr<R>(A.im, emax);
-        out[off + (int64_t)i0 * a.out_st] = o;
-      }
-      if (i1 < nvalid) {
-        MC o;
-        o.x = outr<R>(B.re, emax);
-        o.y = outr<R>(B.im, emax);
-        out[off + (int64_t)i1 * a.out_st] = o;
+      if (IO::kDD && a.out_dd) {
+        float4* o4 = reinterpret_cast<float4*>(out);
+        if (i0 < nvalid) o4[off + (int64_t)i0 * a.out_st] = st_dd4(A);
+        if (i1 < nvalid) o4[off + (int64_t)i1 * a.out_st] = st_dd4(B);
+      } else {
+        if (i0 < nvalid) {
+          MC o;
+          o.x = outr<R>(A.re, emax);
+          o.y = outr<R>(A.im, emax);
+          out[off + (int64_t)i0 * a.out_st] = o;
+        }
+        if (i1 < nvalid) {
+          MC o;
+          o.x = outr<R>(B.re, emax);
+          o.y = outr<R>(B.im, emax);
+          out[off + (int64_t)i1 * a.out_st] = o;
+        }
       }
     }
   } else {  // C2R with a transposed output layout

@@ -103,6 +103,9 @@ struct Pass {
   const void* r2rtw = nullptr;
   // register Stockham kernel for power-of-two lines (fast_pass)
   bool fast = false;
+  // Float64 fast passes: dd-form input / output between consecutive dd passes,
+  // and an exponent reduction over the input before the first pass of a run
+  bool in_dd = false, out_dd = false, reduce_before = false;
   int logm = 0;
   const void* ftw = nullptr;  // its twiddle table (float or dd entries)
   // launch geometry
@@ -136,6 +139,7 @@ struct pfgb_plan {
   int64_t scratch_bytes[2] = {0, 0};
   std::vector<void*> allocations;
   std::map<std::string, void*> tables;
+  int* emax_dev = nullptr;  // scale exponent of the current run of dd passes
   int device = 0;
   bool query_only = false;  // plan analysed on the host only (no device memory)
   // opt-in per-launch timing: (direction, pass index, start, stop)
@@ -529,6 +533,9 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.lmap_tile = A.in_tfast;
   F.out_tfast = A.out_tfast;
   F.store_direct = A.in_tfast ? A.out_tfast : (A.out_sa == 1 ? 1 : 0);
+  F.in_dd = ps.in_dd ? 1 : 0;
+  F.out_dd = ps.out_dd ? 1 : 0;
+  F.emax_ptr = P->emax_dev;
   F.scale_on = scale_on ? 1 : 0;
   const ld sc = 1.0L / (ld)P->scale;
   F.scale_h = (float)sc;
@@ -572,6 +579,7 @@ int launch_pass(int real_bytes, const PassArgs& A, int64_t grid, int threads, si
 int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_emax(const void* x, int64_t n, int* out, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Schedule: build the passes of one direction and assign buffers.
@@ -815,6 +823,20 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
     const void* in = buf(ps.bin);
     void* out = buf(ps.bout);
     if (ps.pk == PK_COPY && in == out && ps.lin.same_order(ps.lout)) continue;
+    if (ps.fast && ps.reduce_before) {
+      pfgb_plan::Rec rr{dsign, 100 + i, nullptr, nullptr};
+      if (P->timing) {
+        PFGB_CUDA(cudaEventCreate(&rr.a));
+        PFGB_CUDA(cudaEventCreate(&rr.b));
+        PFGB_CUDA(cudaEventRecord(rr.a, s));
+      }
+      int rc = launch_emax(in, ps.lin.bytes() / 8, P->emax_dev, s);
+      if (rc) return rc;
+      if (P->timing) {
+        PFGB_CUDA(cudaEventRecord(rr.b, s));
+        P->recs.push_back(rr);
+      }
+    }
     pfgb_plan::Rec rec{dsign, i, nullptr, nullptr};
     if (P->timing) {
       PFGB_CUDA(cudaEventCreate(&rec.a));
@@ -982,6 +1004,24 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   for (auto* dir : {&P->fwd, &P->bwd})
     for (auto& ps : dir->passes)
       if (!rc) rc = prepare_pass(P, ps);
+  // Float64 runs of consecutive fast passes exchange data in dd form
+  if (!rc && P->rb == 8) {
+    for (auto* dir : {&P->fwd, &P->bwd}) {
+      auto& v = dir->passes;
+      for (size_t i = 0; i < v.size(); ++i) {
+        if (!v[i].fast) continue;
+        const bool prev = i > 0 && v[i - 1].fast;
+        const bool next = i + 1 < v.size() && v[i + 1].fast;
+        v[i].in_dd = prev;
+        v[i].out_dd = next;
+        v[i].reduce_before = !prev;
+      }
+    }
+    if (!query_only) {
+      cudaError_t e = cudaMalloc(&P->emax_dev, 16);
+      if (e != cudaSuccess) rc = fail(PFGB_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+  }
   if (!rc && !query_only) {
     for (int s = 0; s < 2; ++s) {
       if (P->scratch_bytes[s] > 0) {
@@ -1040,11 +1080,12 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     std::memset(&e, 0, sizeof(e));
     e.direction = dir;
     e.pass = pass;
-    const Pass& ps = (dir > 0 ? P->fwd : P->bwd).passes[pass];
+    const bool red = pass >= 100;
+    const Pass& ps = (dir > 0 ? P->fwd : P->bwd).passes[red ? pass - 100 : pass];
     e.axis = ps.axis;
-    e.op = ps.pk == PK_COPY ? -1 : ps.op;
-    e.bytes_per_launch = ps.lin.bytes() + ps.lout.bytes();
-    const char* kname = ps.pk == PK_COPY ? "copy_kernel"
+    e.op = red ? -2 : ps.pk == PK_COPY ? -1 : ps.op;
+    e.bytes_per_launch = red ? ps.lin.bytes() : ps.lin.bytes() + ps.lout.bytes();
+    const char* kname = red ? "emax_kernel" : ps.pk == PK_COPY ? "copy_kernel"
                         : ps.fast ? (P->rb == 8 ? "fast_pass<dd>" : "fast_pass<float>")
                                   : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);
@@ -1071,6 +1112,7 @@ int pfgb_plan_destroy(pfgb_plan* P) {
   for (int s = 0; s < 2; ++s)
     if (P->scratch[s]) cudaFree(P->scratch[s]);
   for (auto& kv : P->tables) cudaFree(kv.second);
+  if (P->emax_dev) cudaFree(P->emax_dev);
   delete P;
   return PFGB_OK;
 }

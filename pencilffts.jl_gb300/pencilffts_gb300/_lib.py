@@ -91,19 +91,27 @@ SIGNATURES = {
 }
 
 _LIB = None
+_BUILD_ERROR = None
 
 
 def lib_path() -> str:
-    return _build.LIB
+    """The in-tree library, or the file named by PENCILFFT_GB300_LIB."""
+    return os.environ.get("PENCILFFT_GB300_LIB") or _build.LIB
 
 
 def load(build_if_missing: bool = True):
     """Loads the shared library (building it first if it is missing or stale)."""
-    global _LIB
+    global _LIB, _BUILD_ERROR
     if _LIB is not None:
         return _LIB
-    if build_if_missing and not _build.up_to_date():
-        _build.build()
+    if _BUILD_ERROR is not None:
+        raise RuntimeError(f"libpencilfft_gb300.so failed to build: {_BUILD_ERROR}")
+    if build_if_missing and not os.environ.get("PENCILFFT_GB300_LIB") and not _build.up_to_date():
+        try:
+            _build.build()
+        except Exception as e:  # keep the first failure; do not rebuild on every call
+            _BUILD_ERROR = str(e)[:2000]
+            raise
     path = lib_path()
     if not os.path.exists(path):
         raise RuntimeError(f"libpencilfft_gb300.so not found at {path}; run the build first")
