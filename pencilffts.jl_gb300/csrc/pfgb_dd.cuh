@@ -9,11 +9,12 @@
 // |lo| <= ulp(hi)/2 where needed.  Relative error per operation is about
 // 2^-47 of the operand magnitudes.
 //
-// Conversions between IEEE doubles and dd use integer operations only (no FP64
-// instruction): d2dd splits the 53-bit significand into a 24-bit hi and the
-// correctly rounded remainder; dd2d rebuilds the double from the two
-// significands.  A power-of-two scale (an exponent offset) keeps any finite
-// double range inside the float exponent range.
+// Conversions between IEEE doubles and dd use integer and FP32 operations
+// only (no FP64 instruction: GB300 runs F2F.F64 conversions at the FP64 rate):
+// d2dd splits the 53-bit significand into a 24-bit hi and the rounded
+// remainder; dd2d rebuilds the double from hi's significand plus lo counted in
+// units of the double's last place.  A power-of-two scale (an exponent
+// offset) keeps any finite double range inside the float exponent range.
 #pragma once
 
 #include <stdint.h>
@@ -87,57 +88,46 @@ __device__ __forceinline__ int dexp_bits(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
-// x * 2^(1023 - emax) as dd.  Values more than 2^126 below 2^(emax-1023)
-// become zero; emax is the largest biased exponent of the tile.
+// x * 2^(1023 - emax) as dd.  hi keeps the top 24 significand bits of x, lo
+// the remaining 29 bits rounded to a float (I2F, then an exact power-of-two
+// scale).  Values more than 2^126 below 2^(emax-1023) become zero; emax is
+// the largest biased exponent of the data being converted.
 __device__ __forceinline__ dd d2dd(double x, int emax) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
   const int e = (int)((hi32 >> 20) & 0x7FF);
   const unsigned sign = hi32 & 0x80000000u;
   const int ef = e - emax + 127;  // biased float exponent of the scaled value
-  if (e == 0 || ef <= 0) return dd(0.0f, 0.0f);
-  if (e == 0x7FF) return dd(__uint_as_float(0x7FC00000u), 0.0f);
-  const unsigned m23 = ((hi32 & 0xFFFFFu) << 3) | (lo32 >> 29);
-  const float h = __uint_as_float(sign | ((unsigned)ef << 23) | m23);
-  // remainder: low 29 significand bits, value r29 * 2^(ef - 127 - 52)
-  const unsigned r29 = lo32 & 0x1FFFFFFFu;
-  float l = 0.0f;
-  if (ef > 52 && r29 != 0) {
-    // correctly rounded float(r29) with two exact 16-bit halves and one FMA
-    const float fh = __uint_as_float(0x4B000000u | (r29 >> 15)) - 8388608.0f;
-    const float fl = __uint_as_float(0x4B000000u | (r29 & 0x7FFFu)) - 8388608.0f;
-    const float r = __fmaf_rn(fh, 32768.0f, fl);
-    l = __fmul_rn(r, __uint_as_float((unsigned)(ef - 52) << 23));
-    l = __uint_as_float(__float_as_uint(l) | sign);
-  }
+  const unsigned m23 = __funnelshift_l(lo32, hi32, 3) & 0x7FFFFFu;
+  float h = __uint_as_float(sign | ((unsigned)ef << 23) | m23);
+  const float r = __uint2float_rn(lo32 & 0x1FFFFFFFu);
+  const float sc = __uint_as_float((unsigned)max(ef - 52, 0) << 23);  // 2^(ef - 179), 0 if ef <= 52
+  float l = __uint_as_float(__float_as_uint(__fmul_rn(r, sc)) | sign);
+  if (ef <= 0 || e == 0) { h = 0.0f; l = 0.0f; }
+  if (e == 0x7FF) h = __uint_as_float(0x7FC00000u);
   return dd(h, l);
 }
 
-// (v.h + v.l) * 2^(emax - 1023) as a double (truncating the last bit at worst).
+// (v.h + v.l) * 2^(emax - 1023) as a double.  After a renormalisation the lo
+// part is converted to an integer count of the double's last place (scale by
+// 2^(179 - eh), F2I) and added to hi's significand, which then needs at most
+// a one-bit shift.
 __device__ __forceinline__ double dd2d(dd v, int emax) {
   v = renorm(v);
-  const unsigned hb = __float_as_uint(v.h), lb = __float_as_uint(v.l);
+  const unsigned hb = __float_as_uint(v.h);
   const int eh = (int)((hb >> 23) & 0xFF);
-  if (eh == 0) return 0.0;
-  if (eh == 0xFF) return __longlong_as_double(0x7FF8000000000000ll);
-  const int el = (int)((lb >> 23) & 0xFF);
-  long long M = (long long)(0x800000u | (hb & 0x7FFFFFu)) << 29;  // bit 52 set
-  if (el != 0) {
-    const long long ml = (long long)(0x800000u | (lb & 0x7FFFFFu));
-    const int sh = el - eh + 29;
-    long long t;
-    if (sh >= 0) t = ml << sh;
-    else t = (sh > -40) ? (ml >> (-sh)) : 0;
-    M = ((hb ^ lb) & 0x80000000u) ? M - t : M + t;
-  }
+  const float su = __uint_as_float((unsigned)min(max(306 - eh, 1), 254) << 23);
+  int li = __float2int_rn(__fmul_rn(v.l, su));
+  if (eh < 52) li = 0;
+  const long long mh = (long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
+  long long M = mh + ((hb >> 31) ? -(long long)li : (long long)li);
   int E = eh - 127 + emax;  // biased double exponent
-  if (M >> 53) { M >>= 1; ++E; }
-  else if (!(M >> 52)) { M <<= 1; --E; }
-  if (E <= 0) return 0.0;
-  if (E >= 0x7FF) E = 0x7FF, M = 0;
-  const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
-                                  ((unsigned long long)E << 52) |
-                                  ((unsigned long long)M & 0xFFFFFFFFFFFFFull);
+  if (M >= (1ll << 53)) { M >>= 1; ++E; }
+  else if (M < (1ll << 52)) { M <<= 1; --E; }
+  unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
+                            ((unsigned long long)E << 52) | ((unsigned long long)M & 0xFFFFFFFFFFFFFull);
+  if (eh == 0 || E <= 0) bits = (unsigned long long)(hb & 0x80000000u) << 32;
+  if (eh == 0xFF || E >= 0x7FF) bits = 0x7FF8000000000000ull;
   return __longlong_as_double((long long)bits);
 }
 #endif

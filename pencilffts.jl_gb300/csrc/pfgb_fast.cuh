@@ -51,10 +51,24 @@ __host__ __device__ constexpr int fast_threads() { return 512; }
 __host__ __device__ constexpr int fast_tw(int logm) {
   return (fast_threads() * 8) >> logm > 0 ? ((fast_threads() * 8) >> logm) : 1;
 }
-__host__ __device__ constexpr int fast_pitch(int logm) { return (1 << logm) + (1 << logm) / 8 + 1; }
+// Shared-memory padding of the exchange buffer: one pad slot every 2^shift
+// elements plus `extra` slots per line.  Chosen per element size and line
+// length with a bank model of the stage writes/reads for both thread mappings
+// (8-byte elements: <= 1.25 wavefronts per access for M >= 128; 16-byte
+// elements: conflict-free for 64 <= M <= 4096).
+__host__ __device__ constexpr int fast_pad_shift(int logm, int ebytes) {
+  return ebytes == 16 ? (logm <= 5 ? 2 : 3) : (logm <= 6 ? 2 : 4);
+}
+__host__ __device__ constexpr int fast_pitch_extra(int logm, int ebytes) {
+  return ebytes == 16 ? (logm == 10 ? 2 : logm == 11 ? 4 : logm == 12 ? 0 : 1)
+                      : (logm == 9 ? 2 : logm == 10 ? 4 : logm == 11 ? 8 : logm == 12 ? 0 : 1);
+}
+__host__ __device__ constexpr int fast_pitch(int logm, int ebytes) {
+  return (1 << logm) + ((1 << logm) >> fast_pad_shift(logm, ebytes)) + fast_pitch_extra(logm, ebytes);
+}
 template <typename R>
 __host__ __device__ constexpr size_t fast_smem(int logm) {
-  return (size_t)fast_tw(logm) * fast_pitch(logm) * sizeof(Cx<R>);
+  return (size_t)fast_tw(logm) * fast_pitch(logm, (int)sizeof(Cx<R>)) * sizeof(Cx<R>);
 }
 
 template <typename R>
@@ -92,9 +106,9 @@ __device__ __forceinline__ R half(R x) {
 
 // Shared-memory slot of element pos of complex line p (padding avoids bank
 // conflicts for the strided stage writes and the across-line accesses).
-template <int LOGM>
+template <int LOGM, int EB>
 __device__ __forceinline__ int sidx(int p, int pos) {
-  return p * fast_pitch(LOGM) + pos + (pos >> 3);
+  return p * fast_pitch(LOGM, EB) + pos + (pos >> fast_pad_shift(LOGM, EB));
 }
 
 template <typename R, int LOGM, int SIGN>
@@ -123,7 +137,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       if (!last) {
         const int base = (b - j) * 8 + j;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) z[sidx<LOGM>(p, base + r * Ls)] = v[r];
+        for (int r = 0; r < 8; ++r) z[sidx<LOGM, (int)sizeof(Cx<R>)>(p, base + r * Ls)] = v[r];
       }
       Ls *= 8;
     } else {
@@ -149,7 +163,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
     if (!last) {
       __syncthreads();
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = z[sidx<LOGM>(p, b + r * T)];
+      for (int r = 0; r < 8; ++r) v[r] = z[sidx<LOGM, (int)sizeof(Cx<R>)>(p, b + r * T)];
       __syncthreads();
     }
   }
@@ -326,7 +340,7 @@ __global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const Fas
 
   // via shared memory: transposed layouts and the r2c split
 #pragma unroll
-  for (int r = 0; r < 8; ++r) z[sidx<LOGM>(p, b + r * T)] = v[r];
+  for (int r = 0; r < 8; ++r) z[sidx<LOGM, (int)sizeof(Cx<R>)>(p, b + r * T)] = v[r];
   __syncthreads();
   const int nth = blockDim.x;
   if (a.op == OP_C2C) {
@@ -336,7 +350,7 @@ __global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const Fas
       int i, k;
       if (a.out_tfast) { i = e % TW; k = e / TW; } else { k = e % M; i = e / M; }
       if (i >= nvalid) continue;
-      const Cx<R> y = apply_scale(z[sidx<LOGM>(i, k)], a);
+      const Cx<R> y = apply_scale(z[sidx<LOGM, (int)sizeof(Cx<R>)>(i, k)], a);
       if (IO::kDD && a.out_dd) {
         reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
       } else {
@@ -353,8 +367,8 @@ __global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const Fas
     for (int e = tid; e < tot; e += nth) {
       int q, k;
       if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % m; q = e / m; }
-      const Cx<R> f = z[sidx<LOGM>(q, k)];
-      const Cx<R> g = conj(z[sidx<LOGM>(q, k == 0 ? 0 : M - k)]);
+      const Cx<R> f = z[sidx<LOGM, (int)sizeof(Cx<R>)>(q, k)];
+      const Cx<R> g = conj(z[sidx<LOGM, (int)sizeof(Cx<R>)>(q, k == 0 ? 0 : M - k)]);
       Cx<R> A = f + g, B = mul_mi(f - g);
       A = apply_scale(mk(half(A.re), half(A.im)), a);
       B = apply_scale(mk(half(B.re), half(B.im)), a);
@@ -385,7 +399,7 @@ __global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const Fas
     for (int e = tid; e < tot; e += nth) {
       int q, k;
       if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % M; q = e / M; }
-      const Cx<R> y = apply_scale(z[sidx<LOGM>(q, k)], a);
+      const Cx<R> y = apply_scale(z[sidx<LOGM, (int)sizeof(Cx<R>)>(q, k)], a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
       if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax);
