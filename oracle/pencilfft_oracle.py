@@ -225,29 +225,33 @@ def input_data_type(real, transforms) -> np.dtype:
 # ---------------------------------------------------------------------------
 # 1D transforms (FFTW definitions, via scipy.fft)
 # ---------------------------------------------------------------------------
+# all host threads for the large test arrays
+_W = -1
+
+
 def _r2r_real(x: np.ndarray, kind: int, axis: int) -> np.ndarray:
     if kind == DHT:
-        F = sfft.fft(x, axis=axis)
+        F = sfft.fft(x, axis=axis, workers=_W)
         return F.real - F.imag
     fam, typ = _R2R_SCIPY[kind]
     f = sfft.dct if fam == "dct" else sfft.dst
-    return f(x, type=typ, axis=axis, norm=None)
+    return f(x, type=typ, axis=axis, norm=None, workers=_W)
 
 
 def transform_1d(tr: Tr, x: np.ndarray, axis: int, n_out: int | None = None,
                  forward_sign: bool = True) -> np.ndarray:
     """Apply one 1D transform along ``axis`` (unnormalised, FFTW semantics)."""
     if tr.name == "FFT":
-        return sfft.fft(x, axis=axis)
+        return sfft.fft(x, axis=axis, workers=_W)
     if tr.name == "BFFT":
-        return sfft.ifft(x, axis=axis, norm="forward")
+        return sfft.ifft(x, axis=axis, norm="forward", workers=_W)
     if tr.name == "RFFT":
         if np.iscomplexobj(x):
             raise ValueError("RFFT needs real input")
-        return sfft.rfft(x, axis=axis)
+        return sfft.rfft(x, axis=axis, workers=_W)
     if tr.name == "BRFFT":
         n = length_output(tr, x.shape[axis]) if n_out is None else n_out
-        return sfft.irfft(x, n=n, axis=axis, norm="forward")
+        return sfft.irfft(x, n=n, axis=axis, norm="forward", workers=_W)
     if tr.name == "R2R":
         if np.iscomplexobj(x):
             return _r2r_real(x.real, tr.kind, axis) + 1j * _r2r_real(x.imag, tr.kind, axis)
