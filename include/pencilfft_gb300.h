@@ -168,6 +168,23 @@ int pfgb_plan_set_timing(pfgb_plan* plan, int on);
  * into `out`; `*n` receives the number of entries. Clears the record. */
 int pfgb_plan_get_timing(pfgb_plan* plan, pfgb_pass_timing* out, int max, int* n);
 
+/* Batched 1D Float64 complex FFT that allocates no device memory.
+ *
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a memory manager that owns the device budget, a latency-critical path that
+ * cannot take cudaMalloc's implicit synchronisation, a host callback where
+ * CUDA allocation is not allowed): transforms `howmany` contiguous lines of
+ * `n` complex doubles (interleaved re, im) from `in` to `out` (in == out
+ * allowed), sign -1 (FFT) or +1 (BFFT, unnormalised), on `stream`, computing
+ * in double-float like the Float64 plans.  Its only scratch is a fixed
+ * 130,816-byte static device array (exponent word + twiddle tables), so n
+ * must be a power of two in [32, 4096]; other sizes return PFGB_ERR_ARGUMENT.
+ * The first call on a device (with it current) resolves the array's address
+ * and fills the tables with a synchronous copy: make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* out, const void* in,
+                       void* stream);
+
 /* Copies the message of the last failure on this thread into buf. Returns the
  * message length. */
 int pfgb_last_error(char* buf, size_t n);

@@ -36,6 +36,8 @@ static int fail(int code, const std::string& msg) {
   return code;
 }
 
+int fail_argument(const std::string& msg) { return fail(PFGB_ERR_ARGUMENT, msg); }
+
 int fail_cuda(cudaError_t e, const char* what) {
   return fail(PFGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
