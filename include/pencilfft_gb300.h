@@ -145,6 +145,19 @@ int pfgb_execute_many(pfgb_plan* plan, int direction, int normalise,
                       void* const* dst, const void* const* src, int n,
                       void* stream);
 
+/* Batched form: records the launches of n transforms (plans[i] applied in
+ * direction[i], +1 forward / -1 backward with normalise[i] as in
+ * pfgb_backward, from src[i] to dst[i]) into one CUDA graph, replayed with a
+ * single pfgb_batch_launch.  Covers the reference's collections of fields
+ * (mul!/ldiv! over tuples and arrays, src/operations.jl:129-152) and any mix
+ * of plans and sizes.  The buffers are fixed at creation; plans must outlive
+ * the batch and must not run concurrently with it (they share scratch). */
+typedef struct pfgb_batch pfgb_batch;
+int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* normalise,
+                      void* const* dst, const void* const* src, int n, pfgb_batch** batch);
+int pfgb_batch_launch(pfgb_batch* batch, void* stream);
+int pfgb_batch_destroy(pfgb_batch* batch);
+
 /* Per-pass timing (replaces the reference's opt-in TimerOutputs sections
  * "PencilFFTs mul!", "FFT", ..., src/operations.jl:27,37,47,250,288,299).
  * When enabled, every kernel launch of the plan is bracketed by CUDA events

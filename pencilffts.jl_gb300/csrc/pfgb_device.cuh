@@ -14,9 +14,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pencilfft_gb300.h"
+
 namespace pfgb {
 
 constexpr int kMaxStages = 8;
+constexpr int kMaxDevicesConfigured = 64;  // devices per process the launchers track
 constexpr int kMaxOuter = 12;
 
 // Operation performed by a pass.
@@ -591,6 +594,24 @@ __global__ void copy_kernel(const CopyArgs a) {
     }
     out[oo] = in[io];
   }
+}
+
+int fail_cuda(cudaError_t e, const char* what);
+
+// Shared-memory opt-in of a kernel on the current device, once per device.
+// Plans call every launcher once with grid == 0 at creation ("configure
+// only"), so kernel launches recorded into a CUDA graph never configure.
+template <typename K>
+inline int ensure_smem_attr(K* kernel, int bytes, bool* done, const char* what) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevicesConfigured) return fail_cuda(cudaErrorInvalidDevice, what);
+  if (!done[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return fail_cuda(e, what);
+    done[dev] = true;
+  }
+  return PFGB_OK;
 }
 
 }  // namespace pfgb

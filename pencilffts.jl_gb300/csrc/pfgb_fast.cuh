@@ -46,10 +46,21 @@ struct FastArgs {
   int64_t osz[kMaxOuter], in_so[kMaxOuter], out_so[kMaxOuter];
 };
 
-__host__ __device__ constexpr int fast_threads() { return 512; }
-// complex lines per CTA for a line of 2^logm points
+#ifndef PFGB_FAST_THREADS_F32
+#define PFGB_FAST_THREADS_F32 512
+#endif
+#ifndef PFGB_FAST_THREADS_DD
+#define PFGB_FAST_THREADS_DD 512
+#endif
+// threads per CTA of the fast pass (8 points of one line per thread)
+template <typename R>
+__host__ __device__ constexpr int fast_threads() {
+  return sizeof(R) == 4 ? PFGB_FAST_THREADS_F32 : PFGB_FAST_THREADS_DD;
+}
+// complex lines per CTA for a line of 2^logm points (one line at least)
+template <typename R>
 __host__ __device__ constexpr int fast_tw(int logm) {
-  return (fast_threads() * 8) >> logm > 0 ? ((fast_threads() * 8) >> logm) : 1;
+  return (fast_threads<R>() * 8) >> logm > 0 ? ((fast_threads<R>() * 8) >> logm) : 1;
 }
 // Shared-memory padding of the exchange buffer: one pad slot every 2^shift
 // elements plus `extra` slots per line.  Chosen per element size and line
@@ -68,7 +79,7 @@ __host__ __device__ constexpr int fast_pitch(int logm, int ebytes) {
 }
 template <typename R>
 __host__ __device__ constexpr size_t fast_smem(int logm) {
-  return (size_t)fast_tw(logm) * fast_pitch(logm, (int)sizeof(Cx<R>)) * sizeof(Cx<R>);
+  return (size_t)fast_tw<R>(logm) * fast_pitch(logm, (int)sizeof(Cx<R>)) * sizeof(Cx<R>);
 }
 
 template <typename R>
@@ -206,21 +217,24 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 #ifndef PFGB_FAST_F32_MINBLOCKS
 #define PFGB_FAST_F32_MINBLOCKS 2
 #endif
+#ifndef PFGB_FAST_DD_MINBLOCKS
+#define PFGB_FAST_DD_MINBLOCKS 1
+#endif
 // float tiles fit two CTAs per SM at 64 registers per thread; dd needs more
 // registers and runs one 512-thread CTA per SM.
 template <typename R>
 __host__ __device__ constexpr int fast_min_blocks() {
-  return std::is_same<R, float>::value ? PFGB_FAST_F32_MINBLOCKS : 1;
+  return std::is_same<R, float>::value ? PFGB_FAST_F32_MINBLOCKS : PFGB_FAST_DD_MINBLOCKS;
 }
 
 template <typename R, int LOGM, int SIGN>
-__global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const FastArgs a) {
+__global__ void __launch_bounds__(fast_threads<R>(), fast_min_blocks<R>()) fast_pass(const FastArgs a) {
   using IO = FastIO<R>;
   using MR = typename IO::MR;
   using MC = typename IO::MC;
   constexpr int M = 1 << LOGM;
   constexpr int T = M / 8;
-  constexpr int TW = fast_tw(LOGM);
+  constexpr int TW = fast_tw<R>(LOGM);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
 
@@ -296,8 +310,10 @@ __global__ void __launch_bounds__(512, fast_min_blocks<R>()) fast_pass(const Fas
         B = mk(mkr<R>(rb.x, emax), mkr<R>(rb.y, emax));
       }
       if (k == 0 || 2 * k == M) { A.im = R(0); B.im = R(0); }
-      // pos < m: A + iB ; else conj(A) + i conj(B)
-      v[r] = pos < m ? mk(A.re - B.im, A.im + B.re) : mk(A.re + B.im, B.re - A.im);
+      // pos < m: A + iB ; else conj(A) + i conj(B): one formula with the
+      // imaginary parts negated for the mirrored half (a free sign flip)
+      if (pos >= m) { A.im = -A.im; B.im = -B.im; }
+      v[r] = mk(A.re - B.im, A.im + B.re);
     }
   }
 

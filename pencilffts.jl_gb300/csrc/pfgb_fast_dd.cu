@@ -10,15 +10,12 @@ int fail_cuda(cudaError_t e, const char* what);
 
 template <int LOGM, int SIGN>
 static int launch_one(const FastArgs& A, int64_t grid, cudaStream_t s) {
-  static bool configured = false;
+  static bool configured[kMaxDevicesConfigured] = {};
   const size_t smem = fast_smem<dd>(LOGM);
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(fast_pass<dd, LOGM, SIGN>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(fast_pass)");
-    configured = true;
-  }
-  fast_pass<dd, LOGM, SIGN><<<(unsigned)grid, fast_threads(), smem, s>>>(A);
+  int rc = ensure_smem_attr(fast_pass<dd, LOGM, SIGN>, (int)smem, configured,
+                            "cudaFuncSetAttribute(fast_pass)");
+  if (rc || grid == 0) return rc;
+  fast_pass<dd, LOGM, SIGN><<<(unsigned)grid, fast_threads<dd>(), smem, s>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda(e, "fast_pass launch");
   return PFGB_OK;

@@ -13,13 +13,9 @@ int fail_cuda(cudaError_t e, const char* what);
 
 template <typename R>
 static int launch_pass_t(const PassArgs& A, int64_t grid, int threads, size_t smem, cudaStream_t s) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(pass_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         200 * 1024);
-    if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(pass_kernel)");
-    configured = true;
-  }
+  static bool configured[kMaxDevicesConfigured] = {};
+  int rc = ensure_smem_attr(pass_kernel<R>, 200 * 1024, configured, "cudaFuncSetAttribute(pass_kernel)");
+  if (rc || grid == 0) return rc;
   pass_kernel<R><<<(unsigned)grid, threads, smem, s>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda(e, "pass_kernel launch");

@@ -148,7 +148,7 @@ extern "C" int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* ou
   A.emax_ptr = emax;
   A.nouter = 0;
   A.nt = howmany;
-  const int tw_lines = fast_tw(lg);
+  const int tw_lines = fast_tw<dd>(lg);
   A.ntiles = (howmany + tw_lines - 1) / tw_lines;
   A.in_sa = A.out_sa = 1;
   A.in_st = A.out_st = n;

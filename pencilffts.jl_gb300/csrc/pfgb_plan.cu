@@ -406,17 +406,19 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   if (rc) return rc;
   // power-of-two c2c / r2c / c2r lines take the register Stockham kernel; on
   // Float64 plans it computes in dd unless native FP64 was requested
+  const int fast_max = 8 * (P->rb == 8 ? fast_threads<dd>() : fast_threads<float>());
   if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && ps.L == 0 && M >= 8 &&
-      M <= 4096 && (M & (M - 1)) == 0 && !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+      M <= 4096 && M <= fast_max && (M & (M - 1)) == 0 &&
+      !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
     ps.fast = true;
     ps.logm = 0;
     while ((1 << ps.logm) < M) ++ps.logm;
     rc = upload_fast_table(P, M, &ps.ftw);
     if (rc) return rc;
     const bool packed = ps.op != OP_C2C;
-    ps.clines = fast_tw(ps.logm);
+    ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm) : fast_tw<float>(ps.logm);
     ps.lines = packed ? 2 * ps.clines : ps.clines;
-    ps.threads = fast_threads();
+    ps.threads = P->rb == 8 ? fast_threads<dd>() : fast_threads<float>();
     ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm) : fast_smem<float>(ps.logm);
     return PFGB_OK;
   }
@@ -1006,6 +1008,25 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   for (auto* dir : {&P->fwd, &P->bwd})
     for (auto& ps : dir->passes)
       if (!rc) rc = prepare_pass(P, ps);
+  // set the shared-memory opt-in of every kernel the plan launches now, so that
+  // executions recorded into a CUDA graph only launch
+  if (!rc && !query_only) {
+    for (auto* dir : {&P->fwd, &P->bwd}) {
+      for (auto& ps : dir->passes) {
+        if (rc || ps.pk != PK_TRANSFORM) continue;
+        if (ps.fast) {
+          FastArgs F;
+          std::memset(&F, 0, sizeof(F));
+          rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
+                          : launch_fast_f32(ps.logm, ps.sign, F, 0, nullptr);
+        } else {
+          PassArgs A;
+          std::memset(&A, 0, sizeof(A));
+          rc = launch_pass(P->rb, A, 0, 0, 0, nullptr);
+        }
+      }
+    }
+  }
   // Float64 runs of consecutive fast passes exchange data in dd form
   if (!rc && P->rb == 8) {
     for (auto* dir : {&P->fwd, &P->bwd}) {
@@ -1169,6 +1190,71 @@ int pfgb_backward(pfgb_plan* P, void* dst, const void* src, void* stream, int no
   int rc = check_buffers(P, dst, src, false);
   if (rc) return rc;
   return execute(P, P->bwd, dst, src, (cudaStream_t)stream, normalise != 0, -1);
+}
+
+struct pfgb_batch {
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int n = 0;
+};
+
+int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* normalise,
+                      void* const* dst, const void* const* src, int n, pfgb_batch** out) {
+  g_last_error.clear();
+  if (!out || n < 1 || !plans || !direction || !dst || !src)
+    return fail(PFGB_ERR_ARGUMENT, "invalid batch description");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!plans[i]) return fail(PFGB_ERR_ARGUMENT, "null plan in batch");
+    if (plans[i]->timing) return fail(PFGB_ERR_ARGUMENT, "disable plan timing before recording a batch");
+    int rc = check_buffers(plans[i], dst[i], src[i], direction[i] >= 0);
+    if (rc) return rc;
+  }
+  pfgb_batch* B = new pfgb_batch();
+  B->n = n;
+  auto cleanup = [&](int rc) {
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    if (B->cap) cudaStreamDestroy(B->cap);
+    delete B;
+    return rc;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+  e = cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e)));
+  int rc = PFGB_OK;
+  for (int i = 0; i < n && !rc; ++i) {
+    pfgb_plan* P = plans[i];
+    rc = direction[i] >= 0 ? execute(P, P->fwd, dst[i], src[i], B->cap, false, 1)
+                           : execute(P, P->bwd, dst[i], src[i], B->cap, normalise && normalise[i], -1);
+  }
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(B->cap, &g);
+  B->graph = g;
+  if (rc) return cleanup(rc);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e)));
+  e = cudaGraphInstantiate(&B->exec, B->graph, 0);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)));
+  *out = B;
+  return PFGB_OK;
+}
+
+int pfgb_batch_launch(pfgb_batch* B, void* stream) {
+  if (!B) return fail(PFGB_ERR_ARGUMENT, "null batch");
+  cudaError_t e = cudaGraphLaunch(B->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(PFGB_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
+int pfgb_batch_destroy(pfgb_batch* B) {
+  if (!B) return PFGB_OK;
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  if (B->cap) cudaStreamDestroy(B->cap);
+  delete B;
+  return PFGB_OK;
 }
 
 int pfgb_execute_many(pfgb_plan* P, int direction, int normalise, void* const* dst,

@@ -6,12 +6,12 @@ The API mirrors the reference's ``PencilFFTPlan`` / ``Transforms`` interface at
 """
 from . import transforms as Transforms
 from ._lib import ArgumentError, LibraryError, load as load_library
-from .plans import (ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
+from .plans import (Batch, ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
                     allocate_input, allocate_output, bmul_, gather, is_inplace,
                     ldiv, ldiv_, mul_, plan_query, scale_factor)
 
 __all__ = [
-    "Transforms", "ArgumentError", "LibraryError", "load_library", "ManyPencilArray",
+    "Transforms", "Batch", "ArgumentError", "LibraryError", "load_library", "ManyPencilArray",
     "Pencil", "PencilArray", "PencilFFTPlan", "Val", "allocate_input", "allocate_output",
     "bmul_", "gather", "is_inplace", "ldiv", "ldiv_", "mul_", "plan_query", "scale_factor",
 ]

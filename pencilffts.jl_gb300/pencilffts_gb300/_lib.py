@@ -83,6 +83,11 @@ SIGNATURES = {
     "pfgb_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
     "pfgb_execute_many": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp),
                                          ctypes.POINTER(_vp), ctypes.c_int, _vp]),
+    "pfgb_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_vp),
+                                         ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_vp)]),
+    "pfgb_batch_launch": (ctypes.c_int, [_vp, _vp]),
+    "pfgb_batch_destroy": (ctypes.c_int, [_vp]),
     "pfgb_plan_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "pfgb_plan_get_timing": (ctypes.c_int, [_vp, ctypes.POINTER(PassTiming), ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_int)]),

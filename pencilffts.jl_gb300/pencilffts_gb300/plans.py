@@ -500,6 +500,61 @@ def _apply(dst, plan, src, forward, normalise):
     return plan._run(dst, src, forward, normalise)
 
 
+class Batch:
+    """Batched form: many transforms recorded once into a CUDA graph and
+    replayed with one launch (``pfgb_batch_create`` / ``pfgb_batch_launch``).
+
+    ``ops`` is a sequence of ``(fn, dst, plan, src)`` with ``fn`` one of
+    ``mul_``, ``ldiv_``, ``bmul_``, exactly as the calls would be written; the
+    arrays are bound at construction and every ``launch()`` repeats all of the
+    recorded transforms on their current contents.
+    """
+
+    def __init__(self, ops):
+        ops = list(ops)
+        if not ops:
+            raise ArgumentError("empty batch")
+        n = len(ops)
+        plans = (ctypes.c_void_p * n)()
+        dirs = (ctypes.c_int * n)()
+        norms = (ctypes.c_int * n)()
+        dsts = (ctypes.c_void_p * n)()
+        srcs = (ctypes.c_void_p * n)()
+        self._keep = []
+        for i, (fn, dst, plan, src) in enumerate(ops):
+            if fn is mul_:
+                plan._check_arrays(src, dst)
+                dirs[i], norms[i] = 1, 0
+            elif fn in (ldiv_, bmul_):
+                plan._check_arrays(dst, src)
+                dirs[i], norms[i] = -1, 1 if fn is ldiv_ else 0
+            else:
+                raise ArgumentError("batch operations are mul_, ldiv_ or bmul_")
+            plans[i] = plan._handle.value
+            dsts[i] = dst.data_ptr()
+            srcs[i] = src.data_ptr()
+            self._keep.append((plan, dst, src))
+        self._L = ops[0][2]._L
+        h = ctypes.c_void_p()
+        _lib.check(self._L.pfgb_batch_create(plans, dirs, norms, dsts, srcs, n, ctypes.byref(h)),
+                   "pfgb_batch_create")
+        self._h = h
+
+    def launch(self, stream=None):
+        if stream is None:
+            stream = _torch().cuda.current_stream().cuda_stream
+        _lib.check(self._L.pfgb_batch_launch(self._h, ctypes.c_void_p(int(stream))), "pfgb_batch_launch")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._L.pfgb_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
 def mul_(dst, plan: PencilFFTPlan, src):
     """``mul!(dst, plan, src)``: forward transform (reference operations.jl:24-31)."""
     return _apply(dst, plan, src, True, False)
