@@ -95,6 +95,18 @@ def time_cpu_oracle(dims, rb, budget_s, max_iters=None):
     return 1e3 * statistics.mean(times), len(times), threads
 
 
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """Max of a per-rank timing over all ranks (the slowest replica sets the
+    step time); identity at one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------------------
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------
@@ -216,11 +228,7 @@ def run_gpu(args, rank, world, local_rank):
     ms_total = e0.elapsed_time(e1)
     timing = plan.get_timing()
     plan.set_timing(False)
-    ms_step = ms_total / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ms_total / args.steps, world, dev)
 
     # ---- roofline of the dominant kernel ----
     per_kernel = {}
@@ -275,11 +283,7 @@ def run_gpu(args, rank, world, local_rank):
             host_out.copy_(u2.data, non_blocking=True)
         f1.record(stream)
         torch.cuda.synchronize()
-        e2e_ms = f0.elapsed_time(f1) / args.steps
-        if world > 1:
-            t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
+        e2e_ms = max_over_ranks(f0.elapsed_time(f1) / args.steps, world, dev)
         nb = host_in.numel() * host_in.element_size()
         e2e = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
 

@@ -108,24 +108,26 @@ __device__ __forceinline__ dd d2dd(double x, int emax) {
   return dd(h, l);
 }
 
-// (v.h + v.l) * 2^(emax - 1023) as a double.  After a renormalisation the lo
-// part is converted to an integer count of the double's last place (scale by
-// 2^(179 - eh), F2I) and added to hi's significand, which then needs at most
-// a one-bit shift.
+// (v.h + v.l) * 2^(emax - 1023) as a double.  After a renormalisation
+// (|lo| <= ulp_float(hi)/2) the double bit pattern of hi is built with integer
+// operations, and lo, converted to an integer count of the double's last place
+// (scale by 2^(179 - eh), F2I), is added to that 64-bit pattern: IEEE bit
+// patterns are monotonic in magnitude, and |lo| is at most 2^28 last places,
+// so the sum stays inside hi's binade except below an exact power of two,
+// where the last place halves (the count is doubled there).
 __device__ __forceinline__ double dd2d(dd v, int emax) {
   v = renorm(v);
-  const unsigned hb = __float_as_uint(v.h);
+  const unsigned hb = __float_as_uint(v.h), lb = __float_as_uint(v.l);
   const int eh = (int)((hb >> 23) & 0xFF);
-  const float su = __uint_as_float((unsigned)min(max(306 - eh, 1), 254) << 23);
+  const int E = eh - 127 + emax;  // biased double exponent of hi
+  const unsigned hw = (hb & 0x80000000u) | ((unsigned)(E & 0xFFF) << 20) | ((hb & 0x7FFFFFu) >> 3);
+  const unsigned lw = hb << 29;
+  const float su = __uint_as_float((unsigned)min(max(306 - eh, 1), 254) << 23);  // 2^(179 - eh)
   int li = __float2int_rn(__fmul_rn(v.l, su));
   if (eh < 52) li = 0;
-  const long long mh = (long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
-  long long M = mh + ((hb >> 31) ? -(long long)li : (long long)li);
-  int E = eh - 127 + emax;  // biased double exponent
-  if (M >= (1ll << 53)) { M >>= 1; ++E; }
-  else if (M < (1ll << 52)) { M <<= 1; --E; }
-  unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
-                            ((unsigned long long)E << 52) | ((unsigned long long)M & 0xFFFFFFFFFFFFFull);
+  int lm = ((hb ^ lb) & 0x80000000u) ? -abs(li) : abs(li);  // change of |value|
+  if ((hb & 0x7FFFFFu) == 0 && lm < 0) lm *= 2;
+  unsigned long long bits = (((unsigned long long)hw << 32) | lw) + (unsigned long long)(long long)lm;
   if (eh == 0 || E <= 0) bits = (unsigned long long)(hb & 0x80000000u) << 32;
   if (eh == 0xFF || E >= 0x7FF) bits = 0x7FF8000000000000ull;
   return __longlong_as_double((long long)bits);

@@ -46,27 +46,29 @@ struct FastArgs {
   int64_t osz[kMaxOuter], in_so[kMaxOuter], out_so[kMaxOuter];
 };
 
+// Threads per CTA of the fast pass (8 points of one line per thread) and
+// CTAs per SM, measured on GB300 (512^3 round trip):
+//   dd:    256 threads, 2 CTAs/SM (~125 registers): the two CTAs' load and
+//          compute phases interleave (5.87 ms against 6.58 ms with one
+//          512-thread CTA); 512 threads when a line needs them (M = 4096).
+//   float: 512 threads, 3 CTAs/SM (register cap 42): 1.75 ms against 1.84 ms
+//          with 2 CTAs/SM and 1.80 ms with four 256-thread CTAs.
 #ifndef PFGB_FAST_THREADS_F32
 #define PFGB_FAST_THREADS_F32 512
 #endif
 #ifndef PFGB_FAST_THREADS_DD
-#define PFGB_FAST_THREADS_DD 512
+#define PFGB_FAST_THREADS_DD 256
 #endif
-// threads per CTA of the fast pass (8 points of one line per thread)
 template <typename R>
-__host__ __device__ constexpr int fast_threads() {
-  return sizeof(R) == 4 ? PFGB_FAST_THREADS_F32 : PFGB_FAST_THREADS_DD;
+__host__ __device__ constexpr int fast_threads(int logm) {
+  return sizeof(R) == 4 ? PFGB_FAST_THREADS_F32
+                        : ((1 << logm) / 8 > PFGB_FAST_THREADS_DD ? (1 << logm) / 8 : PFGB_FAST_THREADS_DD);
 }
 // complex lines per CTA for a line of 2^logm points (one line at least)
 template <typename R>
 __host__ __device__ constexpr int fast_tw(int logm) {
-  return (fast_threads<R>() * 8) >> logm > 0 ? ((fast_threads<R>() * 8) >> logm) : 1;
+  return (fast_threads<R>(logm) * 8) >> logm > 0 ? ((fast_threads<R>(logm) * 8) >> logm) : 1;
 }
-// Shared-memory padding of the exchange buffer: one pad slot every 2^shift
-// elements plus `extra` slots per line.  Chosen per element size and line
-// length with a bank model of the stage writes/reads for both thread mappings
-// (8-byte elements: <= 1.25 wavefronts per access for M >= 128; 16-byte
-// elements: conflict-free for 64 <= M <= 4096).
 __host__ __device__ constexpr int fast_pad_shift(int logm, int ebytes) {
   return ebytes == 16 ? (logm <= 5 ? 2 : 3) : (logm <= 6 ? 2 : 4);
 }
@@ -215,20 +217,15 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 }
 
 #ifndef PFGB_FAST_F32_MINBLOCKS
-#define PFGB_FAST_F32_MINBLOCKS 2
+#define PFGB_FAST_F32_MINBLOCKS 3
 #endif
-#ifndef PFGB_FAST_DD_MINBLOCKS
-#define PFGB_FAST_DD_MINBLOCKS 1
-#endif
-// float tiles fit two CTAs per SM at 64 registers per thread; dd needs more
-// registers and runs one 512-thread CTA per SM.
 template <typename R>
-__host__ __device__ constexpr int fast_min_blocks() {
-  return std::is_same<R, float>::value ? PFGB_FAST_F32_MINBLOCKS : PFGB_FAST_DD_MINBLOCKS;
+__host__ __device__ constexpr int fast_min_blocks(int logm) {
+  return sizeof(R) == 4 ? PFGB_FAST_F32_MINBLOCKS : (fast_threads<R>(logm) <= 256 ? 2 : 1);
 }
 
 template <typename R, int LOGM, int SIGN>
-__global__ void __launch_bounds__(fast_threads<R>(), fast_min_blocks<R>()) fast_pass(const FastArgs a) {
+__global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM)) fast_pass(const FastArgs a) {
   using IO = FastIO<R>;
   using MR = typename IO::MR;
   using MC = typename IO::MC;

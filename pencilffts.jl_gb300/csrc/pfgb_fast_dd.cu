@@ -15,7 +15,7 @@ static int launch_one(const FastArgs& A, int64_t grid, cudaStream_t s) {
   int rc = ensure_smem_attr(fast_pass<dd, LOGM, SIGN>, (int)smem, configured,
                             "cudaFuncSetAttribute(fast_pass)");
   if (rc || grid == 0) return rc;
-  fast_pass<dd, LOGM, SIGN><<<(unsigned)grid, fast_threads<dd>(), smem, s>>>(A);
+  fast_pass<dd, LOGM, SIGN><<<(unsigned)grid, fast_threads<dd>(LOGM), smem, s>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda(e, "fast_pass launch");
   return PFGB_OK;

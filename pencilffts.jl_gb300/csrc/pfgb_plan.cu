@@ -406,9 +406,8 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   if (rc) return rc;
   // power-of-two c2c / r2c / c2r lines take the register Stockham kernel; on
   // Float64 plans it computes in dd unless native FP64 was requested
-  const int fast_max = 8 * (P->rb == 8 ? fast_threads<dd>() : fast_threads<float>());
   if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && ps.L == 0 && M >= 8 &&
-      M <= 4096 && M <= fast_max && (M & (M - 1)) == 0 &&
+      M <= 4096 && (M & (M - 1)) == 0 &&
       !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
     ps.fast = true;
     ps.logm = 0;
@@ -418,7 +417,7 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
     const bool packed = ps.op != OP_C2C;
     ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm) : fast_tw<float>(ps.logm);
     ps.lines = packed ? 2 * ps.clines : ps.clines;
-    ps.threads = P->rb == 8 ? fast_threads<dd>() : fast_threads<float>();
+    ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm) : fast_threads<float>(ps.logm);
     ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm) : fast_smem<float>(ps.logm);
     return PFGB_OK;
   }
