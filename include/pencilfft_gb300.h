@@ -138,6 +138,21 @@ int pfgb_forward(pfgb_plan* plan, void* dst, const void* src, void* stream);
 int pfgb_backward(pfgb_plan* plan, void* dst, const void* src, void* stream,
                   int normalise);
 
+/* Spectral derivative fused into the transform (the callers of the reference's
+ * examples/gradient.jl and test/include/FourierOperations.jl, which multiply
+ * the spectrum by i k before ldiv!).  pfgb_forward_deriv computes
+ * i k_dim * (plan * src); pfgb_backward_deriv computes plan \ (i k_dim * src)
+ * (bmul! when normalise == 0) without modifying src.  k = 2 pi f / length with
+ * f the fftfreq / rfftfreq frequency of the index along logical dimension
+ * `dim` (0-based), which must carry FFT, BFFT, RFFT or BRFFT.  The multiply is
+ * applied in the last forward / first backward pass, so it costs no extra
+ * sweep; that pass must be complex-to-complex (PFGB_ERR_UNSUPPORTED if not,
+ * e.g. for 1D r2c plans). */
+int pfgb_forward_deriv(pfgb_plan* plan, void* dst, const void* src, void* stream, int dim,
+                       double length);
+int pfgb_backward_deriv(pfgb_plan* plan, void* dst, const void* src, void* stream, int normalise,
+                        int dim, double length);
+
 /* Applies one plan to a collection of arrays (reference mul!/ldiv!/bmul!
  * broadcast over tuples or arrays of PencilArrays, src/operations.jl:129-152).
  * direction: +1 forward, -1 backward; normalise as in pfgb_backward. */

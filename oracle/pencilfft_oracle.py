@@ -347,6 +347,26 @@ class OraclePlan:
         return self.bmul(v) / self.scale
 
 
+def wavenumbers(plan: "OraclePlan", dim: int, length: float) -> np.ndarray:
+    """i k along 0-based ``dim`` of the plan's spectral (output) array,
+    broadcastable to its logical shape: k = 2 pi f / length with f the
+    AbstractFFTs frequencies (``rfftfreq`` along an r2c / c2r dimension,
+    ``fftfreq`` otherwise), as the reference's test helpers use them
+    (test/include/Grids.jl:38-59)."""
+    tr = plan.transforms[dim]
+    if tr.name == "RFFT":
+        f = np.arange(plan.dims_out[dim])
+    elif tr.name == "BRFFT":
+        f = np.arange(plan.dims[dim])
+    else:
+        n = plan.dims[dim]
+        f = np.fft.fftfreq(n, 1.0 / n)
+    k = 2 * np.pi * f / length
+    shape = [1] * (plan.ndims + len(plan.extra_dims))
+    shape[dim] = -1
+    return (1j * k).reshape(shape)
+
+
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     """Relative L2 error ``|a - b| / |b|`` computed in long double."""
     a = np.asarray(a).astype(np.clongdouble)

@@ -63,6 +63,11 @@ struct PassArgs {
   int64_t in_sa, in_st, out_sa, out_st;  // axis and tile strides (elements)
   int64_t osz[kMaxOuter], in_so[kMaxOuter], out_so[kMaxOuter];
   double scale;
+  // spectral derivative (c2c passes), as in FastArgs: multiply the input
+  // (deriv == 1) or the output (deriv == 2) by i k0 f(index)
+  int deriv, deriv_role, deriv_half;
+  int64_t deriv_n;
+  double k0;
 };
 
 template <typename R>
@@ -426,12 +431,19 @@ __global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
   int64_t rest = bid / a.ntiles;
   const int64_t t0 = tile * a.lines;
   int64_t ioff = t0 * a.in_st, ooff = t0 * a.out_st;
+  int64_t didx = 0;
   for (int d = 0; d < a.nouter; ++d) {
     const int64_t idx = rest % a.osz[d];
     rest /= a.osz[d];
     ioff += idx * a.in_so[d];
     ooff += idx * a.out_so[d];
+    if (a.deriv && a.deriv_role == 2 + d) didx = idx;
   }
+  auto ik = [&](Cx<R> y, int64_t idx) {
+    const int64_t f = (a.deriv_half || idx <= (a.deriv_n - 1) / 2) ? idx : idx - a.deriv_n;
+    const R k = R(a.k0 * (double)f);
+    return mk(-(y.im * k), y.re * k);
+  };
   const int nvalid = (int)min((int64_t)a.lines, a.nt - t0);
   const int Lc = a.L > 0 ? a.L : a.M;
 
@@ -451,6 +463,8 @@ __global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
       if (a.in_tfast) { i = e % a.lines; j = e / a.lines; } else { j = e % a.n_in; i = e / a.n_in; }
       Cx<R> x = mk(R(0), R(0));
       if (i < nvalid) x = in[(int64_t)j * a.in_sa + (int64_t)i * a.in_st];
+      if (a.deriv == 1)
+        x = ik(x, a.deriv_role == 0 ? (int64_t)j : a.deriv_role == 1 ? t0 + i : didx);
       Cx<R>* zl = z + (size_t)i * a.lp;
       if (op == OP_C2C) zl[j] = x; else r2r_pre(zl, a, j, x);
     }
@@ -528,6 +542,8 @@ __global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
       const Cx<R>* zl = z + (size_t)i * a.lp;
       Cx<R> y = op == OP_C2C ? zl[k] : r2r_post(zl, a, k);
       if (a.scale_on) y = scal(y, sc);
+      if (a.deriv == 2)
+        y = ik(y, a.deriv_role == 0 ? (int64_t)k : a.deriv_role == 1 ? t0 + i : didx);
       out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = y;
     }
   } else if (op == OP_R2C) {

@@ -44,7 +44,30 @@ struct FastArgs {
   int64_t nt, ntiles;
   int64_t in_sa, in_st, out_sa, out_st;
   int64_t osz[kMaxOuter], in_so[kMaxOuter], out_so[kMaxOuter];
+  // Spectral derivative fused into the pass (c2c passes): multiply the input
+  // (deriv == 1) or the output (deriv == 2) by i k, k = k0 * f, where f is the
+  // signed frequency of the element's index along one logical dimension
+  // (AbstractFFTs fftfreq/rfftfreq convention).  deriv_role locates that
+  // dimension: 0 the pass axis, 1 the tile dimension, 2 + o outer dimension o.
+  int deriv, deriv_role, deriv_half;
+  int64_t deriv_n;  // physical length of the dimension (frequency wrap)
+  float k0_h, k0_l;
+  // persistent TMA form (fast_pass_tma): tiles of the pass and an error word
+  // set when a wait for a tile's copies gives up
+  int64_t total;
+  int* err;
 };
+
+// i k y for the frequency of index idx (fftfreq: idx - n above (n-1)/2,
+// except along a half-spectrum dimension)
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_ik(Cx<R> y, int64_t idx, int half, int64_t n, float k0h, float k0l) {
+  const int64_t f = (half || idx <= (n - 1) / 2) ? idx : idx - n;
+  R k;
+  if constexpr (std::is_same<R, dd>::value) k = dd(k0h, k0l) * dd((float)f, 0.0f);
+  else k = k0h * (float)f;
+  return mk(-(y.im * k), y.re * k);
+}
 
 // Threads per CTA of the fast pass (8 points of one line per thread) and
 // CTAs per SM, measured on GB300 (512^3 round trip):
@@ -69,19 +92,26 @@ template <typename R>
 __host__ __device__ constexpr int fast_tw(int logm) {
   return (fast_threads<R>(logm) * 8) >> logm > 0 ? ((fast_threads<R>(logm) * 8) >> logm) : 1;
 }
+// Shared-memory padding of the exchange buffer: one pad slot every 2^shift
+// elements plus `extra` slots per line.  Chosen from a bank model of the stage
+// writes/reads for both thread mappings; the best extra depends on the element
+// size and on the lines per CTA (tw).  8-byte elements: <= 1.25 wavefronts
+// per access for M >= 128; 16-byte elements: conflict-free for M >= 64.
 __host__ __device__ constexpr int fast_pad_shift(int logm, int ebytes) {
   return ebytes == 16 ? (logm <= 5 ? 2 : 3) : (logm <= 6 ? 2 : 4);
 }
-__host__ __device__ constexpr int fast_pitch_extra(int logm, int ebytes) {
-  return ebytes == 16 ? (logm == 10 ? 2 : logm == 11 ? 4 : logm == 12 ? 0 : 1)
-                      : (logm == 9 ? 2 : logm == 10 ? 4 : logm == 11 ? 8 : logm == 12 ? 0 : 1);
+__host__ __device__ constexpr int fast_pitch_extra(int tw, int ebytes) {
+  return ebytes == 16 ? (tw >= 8 ? 1 : tw == 4 ? 2 : tw == 2 ? 4 : 0)
+                      : (tw >= 16 ? 1 : tw == 8 ? 2 : tw == 4 ? 4 : tw == 2 ? 8 : 0);
 }
-__host__ __device__ constexpr int fast_pitch(int logm, int ebytes) {
-  return (1 << logm) + ((1 << logm) >> fast_pad_shift(logm, ebytes)) + fast_pitch_extra(logm, ebytes);
+template <typename R>
+__host__ __device__ constexpr int fast_pitch(int logm) {
+  return (1 << logm) + ((1 << logm) >> fast_pad_shift(logm, (int)sizeof(Cx<R>))) +
+         fast_pitch_extra(fast_tw<R>(logm), (int)sizeof(Cx<R>));
 }
 template <typename R>
 __host__ __device__ constexpr size_t fast_smem(int logm) {
-  return (size_t)fast_tw<R>(logm) * fast_pitch(logm, (int)sizeof(Cx<R>)) * sizeof(Cx<R>);
+  return (size_t)fast_tw<R>(logm) * fast_pitch<R>(logm) * sizeof(Cx<R>);
 }
 
 template <typename R>
@@ -119,9 +149,9 @@ __device__ __forceinline__ R half(R x) {
 
 // Shared-memory slot of element pos of complex line p (padding avoids bank
 // conflicts for the strided stage writes and the across-line accesses).
-template <int LOGM, int EB>
+template <typename R, int LOGM>
 __device__ __forceinline__ int sidx(int p, int pos) {
-  return p * fast_pitch(LOGM, EB) + pos + (pos >> fast_pad_shift(LOGM, EB));
+  return p * fast_pitch<R>(LOGM) + pos + (pos >> fast_pad_shift(LOGM, (int)sizeof(Cx<R>)));
 }
 
 template <typename R, int LOGM, int SIGN>
@@ -150,7 +180,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       if (!last) {
         const int base = (b - j) * 8 + j;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) z[sidx<LOGM, (int)sizeof(Cx<R>)>(p, base + r * Ls)] = v[r];
+        for (int r = 0; r < 8; ++r) z[sidx<R, LOGM>(p, base + r * Ls)] = v[r];
       }
       Ls *= 8;
     } else {
@@ -176,7 +206,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
     if (!last) {
       __syncthreads();
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = z[sidx<LOGM, (int)sizeof(Cx<R>)>(p, b + r * T)];
+      for (int r = 0; r < 8; ++r) v[r] = z[sidx<R, LOGM>(p, b + r * T)];
       __syncthreads();
     }
   }
@@ -224,36 +254,41 @@ __host__ __device__ constexpr int fast_min_blocks(int logm) {
   return sizeof(R) == 4 ? PFGB_FAST_F32_MINBLOCKS : (fast_threads<R>(logm) <= 256 ? 2 : 1);
 }
 
+// One tile of a pass: load (from `src`: the pass input in global memory, or
+// a copy of the tile's input lines in shared memory), stages, store.  `src`
+// is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
+// offset in the pass input).
 template <typename R, int LOGM, int SIGN>
-__global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM)) fast_pass(const FastArgs a) {
+__device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
+                                          int64_t soff, int64_t ssa, int64_t sst) {
   using IO = FastIO<R>;
   using MR = typename IO::MR;
   using MC = typename IO::MC;
   constexpr int M = 1 << LOGM;
   constexpr int T = M / 8;
   constexpr int TW = fast_tw<R>(LOGM);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
 
   const int tid = threadIdx.x;
   int p, b;
   if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
 
   // tile decode
-  int64_t bid = blockIdx.x;
   const int64_t tile = bid % a.ntiles;
   int64_t rest = bid / a.ntiles;
   const bool packed = a.op != OP_C2C;
   const int lines = packed ? 2 * TW : TW;
   const int64_t t0 = tile * lines;
   int64_t ioff = t0 * a.in_st, ooff = t0 * a.out_st;
+  int64_t didx = 0;  // index along the derivative dimension when it is an outer one
   for (int d = 0; d < a.nouter; ++d) {
     const int64_t idx = rest % a.osz[d];
     rest /= a.osz[d];
     ioff += idx * a.in_so[d];
     ooff += idx * a.out_so[d];
+    if (a.deriv && a.deriv_role == 2 + d) didx = idx;
   }
   const int nvalid = (int)min((int64_t)lines, a.nt - t0);
+  if (soff >= 0) ioff = soff;
 
   // ---- load: v[r] = line p, element b + r T (stage-1 Stockham inputs) ----
   Cx<R> v[8];
@@ -261,28 +296,35 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
   if constexpr (IO::kDD) emax = *a.emax_ptr;
   if (a.op == OP_C2C) {
     if (IO::kDD && a.in_dd) {
-      const float4* in = reinterpret_cast<const float4*>(a.in) + ioff + (int64_t)p * a.in_st;
+      const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
-        const float4 q = p < nvalid ? in[(int64_t)(b + r * T) * a.in_sa] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : make_float4(0.f, 0.f, 0.f, 0.f);
         v[r] = ld_dd4<R>(q);
       }
     } else {
-      const MC* in = reinterpret_cast<const MC*>(a.in) + ioff + (int64_t)p * a.in_st;
+      const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
-        const MC raw = p < nvalid ? in[(int64_t)(b + r * T) * a.in_sa] : MC{0, 0};
+        const MC raw = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
         v[r] = mk(mkr<R>(raw.x, emax), mkr<R>(raw.y, emax));
       }
     }
+    if (a.deriv == 1) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
+        v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
+      }
+    }
   } else if (a.op == OP_R2C) {
-    const MR* in = reinterpret_cast<const MR*>(a.in) + ioff;
+    const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-      const int64_t off = (int64_t)(b + r * T) * a.in_sa;
-      const MR ra = i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : MR(0);
-      const MR rb = i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : MR(0);
+      const int64_t off = (int64_t)(b + r * T) * ssa;
+      const MR ra = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MR(0);
+      const MR rb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MR(0);
       v[r] = mk(mkr<R>(ra, emax), mkr<R>(rb, emax));
     }
   } else {  // OP_C2R: Hermitian extension of two half spectra, n = M, m = n_in
@@ -292,17 +334,17 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
     for (int r = 0; r < 8; ++r) {
       const int pos = b + r * T;
       const int k = pos < m ? pos : M - pos;
-      const int64_t off = (int64_t)k * a.in_sa;
+      const int64_t off = (int64_t)k * ssa;
       Cx<R> A, B;
       if (IO::kDD && a.in_dd) {
-        const float4* in = reinterpret_cast<const float4*>(a.in) + ioff;
+        const float4* in = reinterpret_cast<const float4*>(src) + ioff;
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        A = ld_dd4<R>(i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : z4);
-        B = ld_dd4<R>(i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : z4);
+        A = ld_dd4<R>(i0 < nvalid ? in[off + (int64_t)i0 * sst] : z4);
+        B = ld_dd4<R>(i1 < nvalid ? in[off + (int64_t)i1 * sst] : z4);
       } else {
-        const MC* in = reinterpret_cast<const MC*>(a.in) + ioff;
-        const MC ra = i0 < nvalid ? in[off + (int64_t)i0 * a.in_st] : MC{0, 0};
-        const MC rb = i1 < nvalid ? in[off + (int64_t)i1 * a.in_st] : MC{0, 0};
+        const MC* in = reinterpret_cast<const MC*>(src) + ioff;
+        const MC ra = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MC{0, 0};
+        const MC rb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MC{0, 0};
         A = mk(mkr<R>(ra.x, emax), mkr<R>(ra.y, emax));
         B = mk(mkr<R>(rb.x, emax), mkr<R>(rb.y, emax));
       }
@@ -318,6 +360,13 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
   fast_stages<R, LOGM, SIGN>(v, z, p, b, a.tw);
 
   // ---- store ----
+  if (a.deriv == 2 && a.store_direct && a.op == OP_C2C) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
+      v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
+    }
+  }
   if (a.store_direct && a.op != OP_R2C) {
     if (a.op == OP_C2C) {
       if (p < nvalid) {
@@ -353,7 +402,7 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
 
   // via shared memory: transposed layouts and the r2c split
 #pragma unroll
-  for (int r = 0; r < 8; ++r) z[sidx<LOGM, (int)sizeof(Cx<R>)>(p, b + r * T)] = v[r];
+  for (int r = 0; r < 8; ++r) z[sidx<R, LOGM>(p, b + r * T)] = v[r];
   __syncthreads();
   const int nth = blockDim.x;
   if (a.op == OP_C2C) {
@@ -363,7 +412,11 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
       int i, k;
       if (a.out_tfast) { i = e % TW; k = e / TW; } else { k = e % M; i = e / M; }
       if (i >= nvalid) continue;
-      const Cx<R> y = apply_scale(z[sidx<LOGM, (int)sizeof(Cx<R>)>(i, k)], a);
+      Cx<R> y = apply_scale(z[sidx<R, LOGM>(i, k)], a);
+      if (a.deriv == 2) {
+        const int64_t idx = a.deriv_role == 0 ? (int64_t)k : a.deriv_role == 1 ? t0 + i : didx;
+        y = mul_ik(y, idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
+      }
       if (IO::kDD && a.out_dd) {
         reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
       } else {
@@ -380,8 +433,8 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
     for (int e = tid; e < tot; e += nth) {
       int q, k;
       if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % m; q = e / m; }
-      const Cx<R> f = z[sidx<LOGM, (int)sizeof(Cx<R>)>(q, k)];
-      const Cx<R> g = conj(z[sidx<LOGM, (int)sizeof(Cx<R>)>(q, k == 0 ? 0 : M - k)]);
+      const Cx<R> f = z[sidx<R, LOGM>(q, k)];
+      const Cx<R> g = conj(z[sidx<R, LOGM>(q, k == 0 ? 0 : M - k)]);
       Cx<R> A = f + g, B = mul_mi(f - g);
       A = apply_scale(mk(half(A.re), half(A.im)), a);
       B = apply_scale(mk(half(B.re), half(B.im)), a);
@@ -412,12 +465,147 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM
     for (int e = tid; e < tot; e += nth) {
       int q, k;
       if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % M; q = e / M; }
-      const Cx<R> y = apply_scale(z[sidx<LOGM, (int)sizeof(Cx<R>)>(q, k)], a);
+      const Cx<R> y = apply_scale(z[sidx<R, LOGM>(q, k)], a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
       if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax);
       if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax);
     }
+  }
+}
+
+template <typename R, int LOGM, int SIGN>
+__global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM)) fast_pass(const FastArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  fast_tile<R, LOGM, SIGN>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent form fed by TMA bulk copies.
+//
+// For passes whose input lines are contiguous (the transformed axis has
+// stride 1) and 16-byte aligned, each CTA walks tiles with a stride of the
+// grid; one thread issues a cp.async.bulk copy per input line of the *next*
+// tile into a shared-memory buffer (two buffers, one mbarrier each), so the
+// HBM reads of tile i+1 proceed while tile i is transformed; the loads of the
+// stage-1 values then come from shared memory.  Waits on the mbarriers are
+// bounded: after ~2^22 polls a CTA records an error in *a.err, waits (bounded)
+// for the copy it issued and leaves.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* ptr) {
+  return (unsigned)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// bytes of one input line and lines of a tile, per operation
+template <typename R, int LOGM>
+__host__ __device__ constexpr int tma_line_bytes(int op) {
+  return op == OP_C2C ? (1 << LOGM) * 2 * (int)sizeof(typename FastIO<R>::MR)
+       : op == OP_R2C ? (1 << LOGM) * (int)sizeof(typename FastIO<R>::MR)
+                      : ((1 << LOGM) / 2 + 1) * 2 * (int)sizeof(typename FastIO<R>::MR);
+}
+template <typename R, int LOGM>
+__host__ __device__ constexpr int tma_tile_bytes(int op) {
+  return ((op == OP_C2C ? fast_tw<R>(LOGM) : 2 * fast_tw<R>(LOGM)) * tma_line_bytes<R, LOGM>(op) + 127) /
+         128 * 128;
+}
+template <typename R, int LOGM>
+__host__ __device__ constexpr size_t tma_smem(int op) {
+  return (fast_smem<R>(LOGM) + 127) / 128 * 128 + 2 * (size_t)tma_tile_bytes<R, LOGM>(op);
+}
+
+template <typename R, int LOGM>
+__device__ __forceinline__ void tma_issue(const FastArgs& a, int64_t bid, unsigned char* buf,
+                                          unsigned long long* bar) {
+  constexpr int TW = fast_tw<R>(LOGM);
+  const int lines = a.op == OP_C2C ? TW : 2 * TW;
+  const int lb = tma_line_bytes<R, LOGM>(a.op);
+  const int esz = a.op == OP_R2C ? (int)sizeof(typename FastIO<R>::MR) : 2 * (int)sizeof(typename FastIO<R>::MR);
+  const int64_t tt = bid % a.ntiles;
+  int64_t rest = bid / a.ntiles;
+  const int64_t t0 = tt * lines;
+  int64_t ioff = t0 * a.in_st;
+  for (int d = 0; d < a.nouter; ++d) {
+    const int64_t idx = rest % a.osz[d];
+    rest /= a.osz[d];
+    ioff += idx * a.in_so[d];
+  }
+  const int nvalid = (int)min((int64_t)lines, a.nt - t0);
+  mbar_expect_tx(bar, (unsigned)(nvalid * lb));
+  const unsigned char* in = reinterpret_cast<const unsigned char*>(a.in);
+  for (int i = 0; i < nvalid; ++i)
+    tma_load_1d(buf + i * lb, in + (ioff + (int64_t)i * a.in_st) * esz, (unsigned)lb, bar);
+}
+
+template <typename R>
+__host__ __device__ constexpr int tma_min_blocks(int logm) {
+  return sizeof(R) == 4 ? 2 : (fast_threads<R>(logm) <= 256 ? 2 : 1);
+}
+
+template <typename R, int LOGM, int SIGN>
+__global__ void __launch_bounds__(fast_threads<R>(LOGM), tma_min_blocks<R>(LOGM)) fast_pass_tma(const FastArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bars[2];
+  __shared__ int s_fail;
+  Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
+  const size_t zb = (fast_smem<R>(LOGM) + 127) / 128 * 128;
+  const int tb = tma_tile_bytes<R, LOGM>(a.op);
+  unsigned char* buf0 = smem_raw + zb;
+  const int line_elems = a.op == OP_C2R ? (1 << LOGM) / 2 + 1 : (1 << LOGM);
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+  }
+  __syncthreads();
+  int64_t tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < a.total) tma_issue<R, LOGM>(a, tile, buf0, &bars[0]);
+  int it = 0;
+  for (; tile < a.total; tile += gridDim.x, ++it) {
+    const int64_t nxt = tile + gridDim.x;
+    if (threadIdx.x == 0 && nxt < a.total)
+      tma_issue<R, LOGM>(a, nxt, buf0 + ((it + 1) & 1) * tb, &bars[(it + 1) & 1]);
+    if (!mbar_wait_bounded(&bars[it & 1], (it >> 1) & 1)) s_fail = 1;
+    __syncthreads();
+    if (s_fail) break;
+    fast_tile<R, LOGM, SIGN>(a, tile, z, buf0 + (it & 1) * tb, 0, 1, line_elems);
+    __syncthreads();
+  }
+  if (s_fail && threadIdx.x == 0) {
+    atomicOr(a.err, 1);
+    // the copy issued for the next tile may still be in flight: wait for it
+    // (bounded) before the CTA's shared memory is released
+    const int64_t nxt = tile + gridDim.x;
+    if (nxt < a.total) mbar_wait_bounded(&bars[(it + 1) & 1], ((it + 1) >> 1) & 1);
   }
 }
 

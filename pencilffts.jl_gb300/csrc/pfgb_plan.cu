@@ -122,6 +122,18 @@ struct Direction {
   std::vector<Pass> passes;
 };
 
+// Spectral derivative fused into a plan execution: multiply the spectrum by
+// i k along logical dimension `dim` (k = 2 pi f / length).  mode 2: on the
+// output of the last forward pass; mode 1: on the input of the first backward
+// pass.
+struct Deriv {
+  int mode = 0;
+  int dim = -1;
+  int64_t n = 0;  // physical length along dim
+  int half = 0;   // 1 along the half-spectrum dimension of r2c / c2r plans
+  double k0 = 0;
+};
+
 }  // namespace pfgb
 
 struct pfgb_plan {
@@ -452,7 +464,7 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
 
 // Fills the kernel arguments of a transform pass for given buffers.
 static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* out, bool scale_on,
-                     PassArgs& A, int64_t& grid) {
+                     PassArgs& A, int64_t& grid, const Deriv* dv = nullptr) {
   std::memset(&A, 0, sizeof(A));
   A.in = in;
   A.out = out;
@@ -518,13 +530,33 @@ static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* o
   }
   A.nouter = no;
   grid = nblocks;
+  if (dv && dv->mode) {
+    int role = -1;
+    if (dv->dim == a) role = 0;
+    else if (dv->dim == t) role = 1;
+    else {
+      int o = 0;
+      for (int q = 0; q < D; ++q) {
+        const int d = ps.lin.perm[q];
+        if (d == a || d == t) continue;
+        if (d == dv->dim) role = 2 + o;
+        ++o;
+      }
+    }
+    if (role < 0) return fail(PFGB_ERR_ARGUMENT, "derivative dimension not found in the pass");
+    A.deriv = dv->mode;
+    A.deriv_role = role;
+    A.deriv_half = dv->half;
+    A.deriv_n = dv->n;
+    A.k0 = dv->k0;
+  }
   return PFGB_OK;
 }
 
 static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, void* out,
-                          bool scale_on, FastArgs& F, int64_t& grid) {
+                          bool scale_on, FastArgs& F, int64_t& grid, const Deriv* dv = nullptr) {
   PassArgs A;
-  int rc = make_args(P, ps, in, out, scale_on, A, grid);
+  int rc = make_args(P, ps, in, out, scale_on, A, grid, dv);
   if (rc) return rc;
   std::memset(&F, 0, sizeof(F));
   F.in = in;
@@ -543,6 +575,12 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   const ld sc = 1.0L / (ld)P->scale;
   F.scale_h = (float)sc;
   F.scale_l = (float)(sc - (ld)F.scale_h);
+  F.deriv = A.deriv;
+  F.deriv_role = A.deriv_role;
+  F.deriv_half = A.deriv_half;
+  F.deriv_n = A.deriv_n;
+  F.k0_h = (float)A.k0;
+  F.k0_l = (float)((ld)A.k0 - (ld)F.k0_h);
   F.nouter = A.nouter;
   F.nt = A.nt;
   F.ntiles = A.ntiles;
@@ -583,6 +621,25 @@ int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_emax(const void* x, int64_t n, int* out, cudaStream_t s);
+int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
+int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
+
+#ifndef PFGB_FAST_TMA
+#define PFGB_FAST_TMA 0
+#endif
+
+// The TMA-fed persistent form needs contiguous input lines (stride 1 along
+// the axis) whose byte length and start addresses are multiples of 16.
+static bool tma_eligible(const pfgb_plan* P, const Pass& ps, const FastArgs& F) {
+  if (!PFGB_FAST_TMA || !ps.fast || F.lmap_tile || F.in_sa != 1) return false;
+  const int esz = F.op == OP_R2C ? P->rb : 2 * P->rb;
+  const int64_t line = (int64_t)(F.op == OP_C2R ? F.n_in : (1 << ps.logm)) * esz;
+  if (line % 16) return false;
+  if ((F.in_st * esz) % 16) return false;
+  for (int d = 0; d < F.nouter; ++d)
+    if ((F.in_so[d] * esz) % 16) return false;
+  return (reinterpret_cast<uintptr_t>(F.in) & 15) == 0;
+}
 
 // ---------------------------------------------------------------------------
 // Schedule: build the passes of one direction and assign buffers.
@@ -808,12 +865,21 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
 }
 
 static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* src,
-                   cudaStream_t s, bool normalise, int dsign) {
+                   cudaStream_t s, bool normalise, int dsign, const Deriv* dv = nullptr) {
   const int m = (int)dir.passes.size();
-  if (m == 0) return PFGB_OK;
-  int last_tr = -1;
+  if (m == 0) return dv && dv->mode ? fail(PFGB_ERR_UNSUPPORTED, "plan has no transform pass") : PFGB_OK;
+  int last_tr = -1, first_tr = -1;
   for (int i = 0; i < m; ++i)
-    if (dir.passes[i].pk == PK_TRANSFORM) last_tr = i;
+    if (dir.passes[i].pk == PK_TRANSFORM) {
+      last_tr = i;
+      if (first_tr < 0) first_tr = i;
+    }
+  const int dpass = dv && dv->mode ? (dv->mode == 2 ? last_tr : first_tr) : -1;
+  if (dv && dv->mode) {
+    if (dpass < 0 || dir.passes[dpass].op != OP_C2C)
+      return fail(PFGB_ERR_UNSUPPORTED, "the fused derivative needs a complex-to-complex pass at that end "
+                                        "of the plan");
+  }
   for (int i = 0; i < m; ++i) {
     const Pass& ps = dir.passes[i];
     auto buf = [&](int b) -> void* {
@@ -854,15 +920,22 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
     } else if (ps.fast) {
       FastArgs F;
       int64_t grid = 0;
-      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid);
+      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr);
       if (rc) return rc;
-      rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, s)
-                      : launch_fast_f32(ps.logm, ps.sign, F, grid, s);
+      if (tma_eligible(P, ps, F)) {
+        F.total = grid;
+        F.err = P->emax_dev + 1;
+        rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, s)
+                        : launch_fast_tma_f32(ps.logm, ps.sign, F, s);
+      } else {
+        rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, s)
+                        : launch_fast_f32(ps.logm, ps.sign, F, grid, s);
+      }
       if (rc) return rc;
     } else {
       PassArgs A;
       int64_t grid = 0;
-      int rc = make_args(P, ps, in, out, normalise && i == last_tr, A, grid);
+      int rc = make_args(P, ps, in, out, normalise && i == last_tr, A, grid, i == dpass ? dv : nullptr);
       if (rc) return rc;
       rc = launch_pass(P->rb, A, grid, ps.threads, ps.smem, s);
       if (rc) return rc;
@@ -1016,8 +1089,12 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
         if (ps.fast) {
           FastArgs F;
           std::memset(&F, 0, sizeof(F));
+          F.op = ps.op;
           rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
                           : launch_fast_f32(ps.logm, ps.sign, F, 0, nullptr);
+          if (!rc && PFGB_FAST_TMA)
+            rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
+                            : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);
         } else {
           PassArgs A;
           std::memset(&A, 0, sizeof(A));
@@ -1039,10 +1116,13 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
         v[i].reduce_before = !prev;
       }
     }
-    if (!query_only) {
-      cudaError_t e = cudaMalloc(&P->emax_dev, 16);
-      if (e != cudaSuccess) rc = fail(PFGB_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    }
+  }
+  // exponent word (Float64 runs) and error word of the TMA-fed passes
+  if (!rc && !query_only) {
+    cudaError_t e = cudaMalloc(&P->emax_dev, 16);
+    if (e != cudaSuccess) rc = fail(PFGB_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    else if ((e = cudaMemset(P->emax_dev, 0, 16)) != cudaSuccess)
+      rc = fail(PFGB_ERR_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
   }
   if (!rc && !query_only) {
     for (int s = 0; s < 2; ++s) {
@@ -1254,6 +1334,39 @@ int pfgb_batch_destroy(pfgb_batch* B) {
   if (B->cap) cudaStreamDestroy(B->cap);
   delete B;
   return PFGB_OK;
+}
+
+static int make_deriv(const pfgb_plan* P, int mode, int dim, double length, Deriv& dv) {
+  if (dim < 0 || dim >= P->N) return fail(PFGB_ERR_ARGUMENT, "derivative dimension out of range");
+  if (!(length > 0)) return fail(PFGB_ERR_ARGUMENT, "domain length must be positive");
+  const int k = P->desc.kind[dim];
+  if (k == PFGB_R2R || k == PFGB_NOTRANSFORM)
+    return fail(PFGB_ERR_ARGUMENT, "a spectral derivative needs an FFT, BFFT, RFFT or BRFFT dimension");
+  dv.mode = mode;
+  dv.dim = dim;
+  dv.half = (k == PFGB_RFFT || k == PFGB_BRFFT) ? 1 : 0;
+  dv.n = k == PFGB_BRFFT ? P->dims_out[dim] : P->dims_in[dim];
+  dv.k0 = 2.0 * 3.14159265358979323846264338327950288 / length;
+  return PFGB_OK;
+}
+
+int pfgb_forward_deriv(pfgb_plan* P, void* dst, const void* src, void* stream, int dim, double length) {
+  int rc = check_buffers(P, dst, src, true);
+  if (rc) return rc;
+  Deriv dv;
+  rc = make_deriv(P, 2, dim, length, dv);
+  if (rc) return rc;
+  return execute(P, P->fwd, dst, src, (cudaStream_t)stream, false, 1, &dv);
+}
+
+int pfgb_backward_deriv(pfgb_plan* P, void* dst, const void* src, void* stream, int normalise, int dim,
+                        double length) {
+  int rc = check_buffers(P, dst, src, false);
+  if (rc) return rc;
+  Deriv dv;
+  rc = make_deriv(P, 1, dim, length, dv);
+  if (rc) return rc;
+  return execute(P, P->bwd, dst, src, (cudaStream_t)stream, normalise != 0, -1, &dv);
 }
 
 int pfgb_execute_many(pfgb_plan* P, int direction, int normalise, void* const* dst,

@@ -408,18 +408,33 @@ class PencilFFTPlan:
         if pout.pencil != self._pencil_out or pout.dtype != self._eltype_out:
             raise ArgumentError("unexpected dimensions of output data")
 
-    def _run(self, dst, src, forward: bool, normalise: bool):
+    def _run(self, dst, src, forward: bool, normalise: bool, deriv=None):
         L = self._L
         stream = self._stream_ptr()
+        d = s = None
+        if deriv is not None:
+            dim, length = deriv
+            if not (1 <= int(dim) <= self.ndims):
+                raise ArgumentError(f"derivative dimension {dim} not in 1:{self.ndims}")
+            d, s = int(dim) - 1, float(length)
         if forward:
             self._check_arrays(src, dst)
-            rc = L.pfgb_forward(self._handle, ctypes.c_void_p(dst.data_ptr()),
-                                ctypes.c_void_p(src.data_ptr()), stream)
+            if d is None:
+                rc = L.pfgb_forward(self._handle, ctypes.c_void_p(dst.data_ptr()),
+                                    ctypes.c_void_p(src.data_ptr()), stream)
+            else:
+                rc = L.pfgb_forward_deriv(self._handle, ctypes.c_void_p(dst.data_ptr()),
+                                          ctypes.c_void_p(src.data_ptr()), stream, d, s)
             _lib.check(rc, "pfgb_forward")
         else:
             self._check_arrays(dst, src)
-            rc = L.pfgb_backward(self._handle, ctypes.c_void_p(dst.data_ptr()),
-                                 ctypes.c_void_p(src.data_ptr()), stream, 1 if normalise else 0)
+            if d is None:
+                rc = L.pfgb_backward(self._handle, ctypes.c_void_p(dst.data_ptr()),
+                                     ctypes.c_void_p(src.data_ptr()), stream, 1 if normalise else 0)
+            else:
+                rc = L.pfgb_backward_deriv(self._handle, ctypes.c_void_p(dst.data_ptr()),
+                                           ctypes.c_void_p(src.data_ptr()), stream,
+                                           1 if normalise else 0, d, s)
             _lib.check(rc, "pfgb_backward")
         return dst
 
@@ -489,15 +504,15 @@ def _check_compatible(a, b):
         raise ArgumentError(f"collections have different lengths: {len(a)} ≠ {len(b)}")
 
 
-def _apply(dst, plan, src, forward, normalise):
+def _apply(dst, plan, src, forward, normalise, deriv=None):
     if _is_collection(dst) or _is_collection(src):
         if not (_is_collection(dst) and _is_collection(src)):
             raise ArgumentError("collections and single arrays cannot be mixed")
         _check_compatible(dst, src)
         for d, s in zip(dst, src):
-            _apply(d, plan, s, forward, normalise)
+            _apply(d, plan, s, forward, normalise, deriv)
         return dst
-    return plan._run(dst, src, forward, normalise)
+    return plan._run(dst, src, forward, normalise, deriv)
 
 
 class Batch:
@@ -555,19 +570,29 @@ class Batch:
             self._h = None
 
 
-def mul_(dst, plan: PencilFFTPlan, src):
-    """``mul!(dst, plan, src)``: forward transform (reference operations.jl:24-31)."""
-    return _apply(dst, plan, src, True, False)
+def mul_(dst, plan: PencilFFTPlan, src, *, deriv=None):
+    """``mul!(dst, plan, src)``: forward transform (reference operations.jl:24-31).
+
+    ``deriv=(dim, L)`` multiplies the output by ``i k_dim`` (the spectral
+    derivative along the 1-based dimension ``dim`` of a periodic domain of
+    length ``L``), fused into the last pass.
+    """
+    return _apply(dst, plan, src, True, False, deriv)
 
 
-def ldiv_(dst, plan: PencilFFTPlan, src):
-    """``ldiv!(dst, plan, src)``: normalised backward transform (operations.jl:44-52)."""
-    return _apply(dst, plan, src, False, True)
+def ldiv_(dst, plan: PencilFFTPlan, src, *, deriv=None):
+    """``ldiv!(dst, plan, src)``: normalised backward transform (operations.jl:44-52).
+
+    ``deriv=(dim, L)`` transforms ``i k_dim * src`` instead (``src`` is not
+    modified): the derivative along ``dim`` in physical space, fused into the
+    first pass (the gradient of examples/gradient.jl without its extra sweep).
+    """
+    return _apply(dst, plan, src, False, True, deriv)
 
 
-def bmul_(dst, plan: PencilFFTPlan, src):
+def bmul_(dst, plan: PencilFFTPlan, src, *, deriv=None):
     """``bmul!(dst, plan, src)``: unnormalised backward transform (operations.jl:34-41)."""
-    return _apply(dst, plan, src, False, False)
+    return _apply(dst, plan, src, False, False, deriv)
 
 
 def ldiv(plan: PencilFFTPlan, src):

@@ -1,0 +1,86 @@
+"""Spectral derivatives fused into the transform (GPU): the multiply by i k of
+the reference's gradient / curl helpers (examples/gradient.jl,
+test/include/FourierOperations.jl) done in the first backward or last forward
+pass, against the oracle; and the Taylor-Green vorticity of
+test/taylor_green.jl:125-150 computed with fused derivatives."""
+import os
+
+import numpy as np
+import pytest
+
+import pencilffts_gb300 as P
+from helpers import T, TOL, input_array, oracle_plan, rel
+from oracle import pencilfft_oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("real", [np.float64, np.float32])
+@pytest.mark.parametrize("dims,tr", [((64, 32, 48), T.RFFT()), ((32, 24, 40), T.FFT()),
+                                     ((30, 20, 12), T.RFFT()), ((16, 32, 64), T.RFFT())],
+                         ids=["rfft-pow2", "fft", "rfft-generic", "rfft-c1"])
+def test_fused_derivative_matches_oracle(cuda, dims, tr, real):
+    plan = P.PencilFFTPlan(dims, tr, real)
+    orc = oracle_plan(plan)
+    rng = np.random.default_rng(9)
+    shape = dims
+    if plan.eltype_input().kind == "c":
+        x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    else:
+        x = rng.standard_normal(shape)
+    x = x.astype(plan.eltype_input())
+    L = (2 * np.pi, 3.0, 5.5)
+    A = input_array(plan, x)
+    for d in range(3):
+        ik = O.wavenumbers(orc, d, L[d])
+        B = plan.allocate_output()
+        P.mul_(B, plan, A, deriv=(d + 1, L[d]))
+        assert rel(B.to_logical(), ik * orc.forward(x)) <= TOL[np.dtype(real)]
+        spec = orc.forward(x)
+        S = plan.allocate_output()
+        S.copy_from_logical(spec)
+        before = S.to_logical()
+        U = plan.allocate_input()
+        P.ldiv_(U, plan, S, deriv=(d + 1, L[d]))
+        assert np.array_equal(S.to_logical(), before)  # the spectrum is not modified
+        assert rel(U.to_logical(), orc.ldiv(ik * spec)) <= TOL[np.dtype(real)]
+
+
+def test_taylor_green_vorticity_fused(cuda):
+    g = np.load(os.path.join(GOLD, "taylor_green_16_8_16.npz"))
+    dims = (16, 8, 16)
+    Ls = tuple(float(v) for v in g["L"])
+    plan = P.PencilFFTPlan(dims, T.RFFT(), np.float64)
+    u = plan.allocate_input(P.Val(3))
+    for c, x in zip(u, g["u"]):
+        c.copy_from_logical(x)
+    uF = plan * u
+    tmp = plan.allocate_input()
+
+    def d(comp, dim):  # physical derivative of component comp along dim (1-based)
+        P.ldiv_(tmp, plan, uF[comp], deriv=(dim, Ls[dim - 1]))
+        return tmp.to_logical()
+    w = [d(2, 2) - d(1, 3), d(0, 3) - d(2, 1), d(1, 1) - d(0, 2)]
+    err = sum(np.sum((wi - wr) ** 2) for wi, wr in zip(w, g["w"]))
+    assert err < 1e-16 * 1e3   # reference test/taylor_green.jl:148-149 (summed squared error)
+    # divergence is zero
+    div = d(0, 1) + d(1, 2) + d(2, 3)
+    assert np.max(np.abs(div)) < 1e-12
+
+
+def test_derivative_errors(cuda):
+    plan = P.PencilFFTPlan((16, 12), (T.R2R(T.REDFT10), T.FFT()), np.float64)
+    A = plan.allocate_input()
+    B = plan.allocate_output()
+    with pytest.raises(P.ArgumentError, match="FFT, BFFT, RFFT or BRFFT"):
+        P.mul_(B, plan, A, deriv=(1, 1.0))
+    with pytest.raises(P.ArgumentError):
+        P.mul_(B, plan, A, deriv=(3, 1.0))
+    # the multiply needs a complex-to-complex pass at that end of the plan
+    plan1 = P.PencilFFTPlan((32,), T.RFFT(), np.float64)
+    with pytest.raises(P.LibraryError, match="complex-to-complex"):
+        P.mul_(plan1.allocate_output(), plan1, plan1.allocate_input(), deriv=(1, 1.0))
+    planb = P.PencilFFTPlan((16, 12, 9), T.BRFFT(16), np.float64)
+    with pytest.raises(P.LibraryError, match="complex-to-complex"):
+        P.mul_(planb.allocate_output(), planb, planb.allocate_input(), deriv=(1, 1.0))
