@@ -625,13 +625,19 @@ int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
 
 #ifndef PFGB_FAST_TMA
-#define PFGB_FAST_TMA 0
+#define PFGB_FAST_TMA 1
 #endif
 
 // The TMA-fed persistent form needs contiguous input lines (stride 1 along
-// the axis) whose byte length and start addresses are multiples of 16.
+// the axis) whose byte length and start addresses are multiples of 16.  It is
+// used for c2r passes only: measured on the 512^3 round trip it is faster
+// there (each input element feeds two positions of the Hermitian extension,
+// so reading the tile from shared memory saves half of the global loads:
+// 1.24 -> 1.11 ms for Float64) and slower on c2c / r2c passes (0.89 -> 1.04 ms,
+// 0.91 -> 1.01 ms), where several resident CTAs already overlap load and
+// compute.
 static bool tma_eligible(const pfgb_plan* P, const Pass& ps, const FastArgs& F) {
-  if (!PFGB_FAST_TMA || !ps.fast || F.lmap_tile || F.in_sa != 1) return false;
+  if (!PFGB_FAST_TMA || !ps.fast || F.op != OP_C2R || F.lmap_tile || F.in_sa != 1) return false;
   const int esz = F.op == OP_R2C ? P->rb : 2 * P->rb;
   const int64_t line = (int64_t)(F.op == OP_C2R ? F.n_in : (1 << ps.logm)) * esz;
   if (line % 16) return false;
