@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include "pencilfft_gb300.h"
+#include "pfgb_div31.h"
 
 namespace pfgb {
 

@@ -44,6 +44,9 @@ struct FastArgs {
   int64_t nt, ntiles;
   int64_t in_sa, in_st, out_sa, out_st;
   int64_t osz[kMaxOuter], in_so[kMaxOuter], out_so[kMaxOuter];
+  // the tile decode's divisors (ntiles, osz[d]) as multiply-and-shift pairs;
+  // tile indices are below 2^31 (checked at launch)
+  Div31 div_tiles, div_osz[kMaxOuter];
   // Spectral derivative fused into the pass (c2c passes): multiply the input
   // (deriv == 1) or the output (deriv == 2) by i k, k = k0 * f, where f is the
   // signed frequency of the element's index along one logical dimension
@@ -71,9 +74,11 @@ __device__ __forceinline__ Cx<R> mul_ik(Cx<R> y, int64_t idx, int half, int64_t 
 
 // Threads per CTA of the fast pass (8 points of one line per thread) and
 // CTAs per SM, measured on GB300 (512^3 round trip):
-//   dd:    256 threads, 2 CTAs/SM (~125 registers): the two CTAs' load and
-//          compute phases interleave (5.87 ms against 6.58 ms with one
-//          512-thread CTA); 512 threads when a line needs them (M = 4096).
+//   dd:    256 threads, 3 CTAs/SM (80 registers): the CTAs' load and
+//          compute phases interleave (two CTAs: 5.87 ms against 6.58 ms with
+//          one 512-thread CTA; three: 5.43 ms against 5.63 ms with two;
+//          128-thread CTAs: 5.81 ms); 512 threads when a line needs them
+//          (M = 4096).
 //   float: 512 threads, 3 CTAs/SM (register cap 42): 1.75 ms against 1.84 ms
 //          with 2 CTAs/SM and 1.80 ms with four 256-thread CTAs.
 #ifndef PFGB_FAST_THREADS_F32
@@ -249,9 +254,18 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 #ifndef PFGB_FAST_F32_MINBLOCKS
 #define PFGB_FAST_F32_MINBLOCKS 3
 #endif
+// dd CTAs of 256 threads: three per SM (80 registers, <= 8 bytes of spill)
+// measured 5.43 ms against 5.63 ms with two (123 registers) per 512^3 round
+// trip; 0 selects 128 registers a thread (512 / threads CTAs).
+#ifndef PFGB_FAST_DD_MINBLOCKS
+#define PFGB_FAST_DD_MINBLOCKS 3
+#endif
 template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm) {
-  return sizeof(R) == 4 ? PFGB_FAST_F32_MINBLOCKS : (fast_threads<R>(logm) <= 256 ? 2 : 1);
+  return sizeof(R) == 4 ? PFGB_FAST_F32_MINBLOCKS
+         : fast_threads<R>(logm) >= 512 ? 1
+         : PFGB_FAST_DD_MINBLOCKS > 0 ? PFGB_FAST_DD_MINBLOCKS
+                                      : 512 / fast_threads<R>(logm);
 }
 
 // One tile of a pass: load (from `src`: the pass input in global memory, or
@@ -272,17 +286,18 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   int p, b;
   if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
 
-  // tile decode
-  const int64_t tile = bid % a.ntiles;
-  int64_t rest = bid / a.ntiles;
+  // tile decode (bid < 2^31: multiply-and-shift divisions)
+  unsigned rest = div31((unsigned)bid, a.div_tiles);
+  const unsigned tile = (unsigned)bid - rest * (unsigned)a.ntiles;
   const bool packed = a.op != OP_C2C;
   const int lines = packed ? 2 * TW : TW;
-  const int64_t t0 = tile * lines;
+  const int64_t t0 = (int64_t)tile * lines;
   int64_t ioff = t0 * a.in_st, ooff = t0 * a.out_st;
   int64_t didx = 0;  // index along the derivative dimension when it is an outer one
   for (int d = 0; d < a.nouter; ++d) {
-    const int64_t idx = rest % a.osz[d];
-    rest /= a.osz[d];
+    const unsigned q = div31(rest, a.div_osz[d]);
+    const int64_t idx = rest - q * (unsigned)a.osz[d];
+    rest = q;
     ioff += idx * a.in_so[d];
     ooff += idx * a.out_so[d];
     if (a.deriv && a.deriv_role == 2 + d) didx = idx;

@@ -150,6 +150,8 @@ extern "C" int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* ou
   A.nt = howmany;
   const int tw_lines = fast_tw<dd>(lg);
   A.ntiles = (howmany + tw_lines - 1) / tw_lines;
+  if (A.ntiles >= (int64_t(1) << 31)) return fail_argument("howmany too large for one launch");
+  A.div_tiles = make_div31(A.ntiles);
   A.in_sa = A.out_sa = 1;
   A.in_st = A.out_st = n;
   return launch_fast_dd(lg, sign, A, A.ntiles, s);

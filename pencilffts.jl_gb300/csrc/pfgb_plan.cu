@@ -588,10 +588,13 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.in_st = A.in_st;
   F.out_sa = A.out_sa;
   F.out_st = A.out_st;
+  if (grid >= (int64_t{1} << 31)) return fail(PFGB_ERR_UNSUPPORTED, "too many tiles in one pass");
+  F.div_tiles = make_div31(A.ntiles);
   for (int d = 0; d < A.nouter; ++d) {
     F.osz[d] = A.osz[d];
     F.in_so[d] = A.in_so[d];
     F.out_so[d] = A.out_so[d];
+    F.div_osz[d] = make_div31(A.osz[d]);
   }
   return PFGB_OK;
 }
@@ -625,17 +628,16 @@ int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
 
 #ifndef PFGB_FAST_TMA
-#define PFGB_FAST_TMA 1
+#define PFGB_FAST_TMA 0
 #endif
 
 // The TMA-fed persistent form needs contiguous input lines (stride 1 along
-// the axis) whose byte length and start addresses are multiples of 16.  It is
-// used for c2r passes only: measured on the 512^3 round trip it is faster
-// there (each input element feeds two positions of the Hermitian extension,
-// so reading the tile from shared memory saves half of the global loads:
-// 1.24 -> 1.11 ms for Float64) and slower on c2c / r2c passes (0.89 -> 1.04 ms,
-// 0.91 -> 1.01 ms), where several resident CTAs already overlap load and
-// compute.
+// the axis) whose byte length and start addresses are multiples of 16, and is
+// written for c2r passes (each input element feeds two positions of the
+// Hermitian extension, so reading the tile from shared memory halves the
+// global loads).  Off by default: with three resident 256-thread CTAs per SM
+// the plain kernel overlaps load and compute better (Float64 512^3 c2r pass
+// 1.05 ms against 1.09 ms; the TMA form's two tile buffers allow two CTAs).
 static bool tma_eligible(const pfgb_plan* P, const Pass& ps, const FastArgs& F) {
   if (!PFGB_FAST_TMA || !ps.fast || F.op != OP_C2R || F.lmap_tile || F.in_sa != 1) return false;
   const int esz = F.op == OP_R2C ? P->rb : 2 * P->rb;
