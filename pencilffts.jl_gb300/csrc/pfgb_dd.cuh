@@ -90,47 +90,61 @@ __device__ __forceinline__ int dexp_bits(double x) {
 
 // x * 2^(1023 - emax) as dd.  hi keeps the top 24 significand bits of x, lo
 // the remaining 29 bits rounded to a float (I2F, then an exact power-of-two
-// scale).  Values more than 2^126 below 2^(emax-1023) become zero; emax is
-// the largest biased exponent of the data being converted.
+// scale).  emax is the largest biased exponent of the data being converted.
+// Common case (finite nonzero x whose scaled float exponent ef lies in
+// [53, 254]): the float pattern of hi is the funnel-shifted word (low 9
+// exponent bits : 23 significand bits) plus (127 - emax) << 23, since
+// (e + 127 - emax) mod 512 = ef.  Rare cases: zero, subnormal and values
+// more than 2^126 below 2^(emax-1023) become zero, Inf/NaN become NaN, and
+// values 2^74..2^126 below keep hi only.
 __device__ __forceinline__ dd d2dd(double x, int emax) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
   const int e = (int)((hi32 >> 20) & 0x7FF);
+  const int c = 127 - emax;  // ef = e + c
+  const int lo = max(53 - c, 1), hi = min(254 - c, 2046);
   const unsigned sign = hi32 & 0x80000000u;
-  const int ef = e - emax + 127;  // biased float exponent of the scaled value
-  const unsigned m23 = __funnelshift_l(lo32, hi32, 3) & 0x7FFFFFu;
-  float h = __uint_as_float(sign | ((unsigned)ef << 23) | m23);
-  const float r = __uint2float_rn(lo32 & 0x1FFFFFFFu);
-  const float sc = __uint_as_float((unsigned)max(ef - 52, 0) << 23);  // 2^(ef - 179), 0 if ef <= 52
-  float l = __uint_as_float(__float_as_uint(__fmul_rn(r, sc)) | sign);
-  if (ef <= 0 || e == 0) { h = 0.0f; l = 0.0f; }
-  if (e == 0x7FF) h = __uint_as_float(0x7FC00000u);
-  return dd(h, l);
+  const unsigned fs = __funnelshift_l(lo32, hi32, 3);
+  if ((unsigned)(e - lo) <= (unsigned)(hi - lo)) {
+    const unsigned hx = fs + ((unsigned)c << 23);
+    const float r = __uint2float_rn(lo32 & 0x1FFFFFFFu);
+    const float sc = __uint_as_float((hx & 0x7F800000u) - (52u << 23));  // 2^(ef - 179)
+    return dd(__uint_as_float(hx | sign), __uint_as_float(__float_as_uint(__fmul_rn(r, sc)) | sign));
+  }
+  const int ef = e + c;
+  if (e == 0x7FF) return dd(__uint_as_float(0x7FC00000u), 0.0f);
+  if (e == 0 || ef <= 0) return dd(0.0f, 0.0f);
+  return dd(__uint_as_float(sign | ((unsigned)ef << 23) | (fs & 0x7FFFFFu)), 0.0f);
 }
 
-// (v.h + v.l) * 2^(emax - 1023) as a double.  After a renormalisation
-// (|lo| <= ulp_float(hi)/2) the double bit pattern of hi is built with integer
-// operations, and lo, converted to an integer count of the double's last place
-// (scale by 2^(179 - eh), F2I), is added to that 64-bit pattern: IEEE bit
-// patterns are monotonic in magnitude, and |lo| is at most 2^28 last places,
-// so the sum stays inside hi's binade except below an exact power of two,
-// where the last place halves (the count is doubled there).
+// (v.h + v.l) * 2^(emax - 1023) as a double, within one unit in the last
+// place.  The renormalised pair s + e (fast two-sum, |e| <= ulp_float(s)/2)
+// gives the double bit pattern of s by integer operations, and e, converted
+// to a signed count of the double's last place (scale by +-2^(179 - es), F2I),
+// is added to that 64-bit pattern: IEEE bit patterns are monotonic in
+// magnitude and |count| <= 2^28, so the sum stays inside s's binade except
+// below an exact power of two, where the last place halves (the count is
+// doubled there).  Rare cases (checked once): s zero or subnormal and
+// results below the double range give zero, Inf/NaN and overflow give NaN.
 __device__ __forceinline__ double dd2d(dd v, int emax) {
-  v = renorm(v);
-  const unsigned hb = __float_as_uint(v.h), lb = __float_as_uint(v.l);
-  const int eh = (int)((hb >> 23) & 0xFF);
-  const int E = eh - 127 + emax;  // biased double exponent of hi
-  const unsigned hw = (hb & 0x80000000u) | ((unsigned)(E & 0xFFF) << 20) | ((hb & 0x7FFFFFu) >> 3);
-  const unsigned lw = hb << 29;
-  const float su = __uint_as_float((unsigned)min(max(306 - eh, 1), 254) << 23);  // 2^(179 - eh)
-  int li = __float2int_rn(__fmul_rn(v.l, su));
-  if (eh < 52) li = 0;
-  int lm = ((hb ^ lb) & 0x80000000u) ? -abs(li) : abs(li);  // change of |value|
-  if ((hb & 0x7FFFFFu) == 0 && lm < 0) lm *= 2;
-  unsigned long long bits = (((unsigned long long)hw << 32) | lw) + (unsigned long long)(long long)lm;
-  if (eh == 0 || E <= 0) bits = (unsigned long long)(hb & 0x80000000u) << 32;
-  if (eh == 0xFF || E >= 0x7FF) bits = 0x7FF8000000000000ull;
-  return __longlong_as_double((long long)bits);
+  const float s = __fadd_rn(v.h, v.l);
+  const float e = __fsub_rn(v.l, __fsub_rn(s, v.h));
+  const unsigned sb = __float_as_uint(s);
+  const unsigned esx = sb & 0x7F800000u;  // float exponent << 23
+  const int es = (int)(esx >> 23);
+  const int off = emax - 127;             // double exponent E = es + off
+  const int lo = max(1 - off, 1), hi = min(2046 - off, 254);
+  const unsigned sign = sb & 0x80000000u;
+  if ((unsigned)(es - lo) <= (unsigned)(hi - lo)) {
+    const unsigned hw = (((sb & 0x7FFFFFFFu) >> 3) + ((unsigned)off << 20)) | sign;
+    const unsigned sux = (0x99000000u - max(esx, 52u << 23)) | sign;  // +-2^(179 - es)
+    int li = __float2int_rn(__fmul_rn(e, __uint_as_float(sux)));
+    if (li < 0 && (sb & 0x7FFFFFu) == 0) li *= 2;
+    const unsigned long long bits = (((unsigned long long)hw << 32) | (sb << 29)) + (unsigned long long)(long long)li;
+    return __longlong_as_double((long long)bits);
+  }
+  if (es == 255 || es + off >= 0x7FF) return __longlong_as_double(0x7FF8000000000000ll);
+  return __longlong_as_double((long long)((unsigned long long)sign << 32));
 }
 #endif
 

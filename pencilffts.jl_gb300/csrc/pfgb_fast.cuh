@@ -40,6 +40,9 @@ struct FastArgs {
   // the run's double input (computed by emax_kernel before the run).
   int in_dd, out_dd;
   const int* emax_ptr;
+  // added to *emax_ptr for the double outputs of the pass: the ldiv!
+  // normalisation when it is a power of two (scale_on is then 0)
+  int emax_shift;
   int nouter;
   int64_t nt, ntiles;
   int64_t in_sa, in_st, out_sa, out_st;
@@ -155,9 +158,18 @@ __device__ __forceinline__ R half(R x) {
 // Shared-memory slot of element pos of complex line p (padding avoids bank
 // conflicts for the strided stage writes and the across-line accesses).
 template <typename R, int LOGM>
-__device__ __forceinline__ int sidx(int p, int pos) {
-  return p * fast_pitch<R>(LOGM) + pos + (pos >> fast_pad_shift(LOGM, (int)sizeof(Cx<R>)));
+__host__ __device__ constexpr int padded(int pos) {
+  return pos + (pos >> fast_pad_shift(LOGM, (int)sizeof(Cx<R>)));
 }
+template <typename R, int LOGM>
+__device__ __forceinline__ int sidx(int p, int pos) {
+  return p * fast_pitch<R>(LOGM) + padded<R, LOGM>(pos);
+}
+// The padding is additive over the exchange patterns: with all sizes powers
+// of two, padded(p0 + r L) = padded(p0) + padded(r L) for 0 <= r < 8 when
+// p0 = b < T = M/8 and L = T (stage reads), and when p0 = 8 Ls m + j with
+// j < Ls and L = Ls (stage writes): a thread forms one base address and
+// reaches its 8 slots at compile-time offsets.
 
 template <typename R, int LOGM, int SIGN>
 __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int b, const void* tw) {
@@ -183,9 +195,9 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       }
       dft8<SIGN>(v);
       if (!last) {
-        const int base = (b - j) * 8 + j;
+        Cx<R>* zw = z + sidx<R, LOGM>(p, (b - j) * 8 + j);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) z[sidx<R, LOGM>(p, base + r * Ls)] = v[r];
+        for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * Ls)] = v[r];
       }
       Ls *= 8;
     } else {
@@ -210,8 +222,9 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
     }
     if (!last) {
       __syncthreads();
+      const Cx<R>* zr = z + sidx<R, LOGM>(p, b);
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = z[sidx<R, LOGM>(p, b + r * T)];
+      for (int r = 0; r < 8; ++r) v[r] = zr[padded<R, LOGM>(r * T)];
       __syncthreads();
     }
   }
@@ -307,8 +320,11 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
 
   // ---- load: v[r] = line p, element b + r T (stage-1 Stockham inputs) ----
   Cx<R> v[8];
-  int emax = 0;
-  if constexpr (IO::kDD) emax = *a.emax_ptr;
+  int emax = 0, emax_out = 0;
+  if constexpr (IO::kDD) {
+    emax = *a.emax_ptr;
+    emax_out = emax + a.emax_shift;
+  }
   if (a.op == OP_C2C) {
     if (IO::kDD && a.in_dd) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
@@ -318,12 +334,14 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         v[r] = ld_dd4<R>(q);
       }
     } else {
+      // all loads first, conversions after: the conversion's rare-case
+      // branch must not serialise the loads
       const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
+      MC raw[8];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        const MC raw = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
-        v[r] = mk(mkr<R>(raw.x, emax), mkr<R>(raw.y, emax));
-      }
+      for (int r = 0; r < 8; ++r) raw[r] = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
     }
     if (a.deriv == 1) {
 #pragma unroll
@@ -335,16 +353,29 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   } else if (a.op == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
+    MR ra[8], rb[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int64_t off = (int64_t)(b + r * T) * ssa;
-      const MR ra = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MR(0);
-      const MR rb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MR(0);
-      v[r] = mk(mkr<R>(ra, emax), mkr<R>(rb, emax));
+      ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MR(0);
+      rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MR(0);
     }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
   } else {  // OP_C2R: Hermitian extension of two half spectra, n = M, m = n_in
     const int m = a.n_in;
     const int i0 = 2 * p, i1 = 2 * p + 1;
+    MC ra[8], rb[8];
+    if (!(IO::kDD && a.in_dd)) {
+      const MC* in = reinterpret_cast<const MC*>(src) + ioff;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int pos = b + r * T;
+        const int64_t off = (int64_t)(pos < m ? pos : M - pos) * ssa;
+        ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MC{0, 0};
+        rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MC{0, 0};
+      }
+    }
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int pos = b + r * T;
@@ -357,11 +388,8 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         A = ld_dd4<R>(i0 < nvalid ? in[off + (int64_t)i0 * sst] : z4);
         B = ld_dd4<R>(i1 < nvalid ? in[off + (int64_t)i1 * sst] : z4);
       } else {
-        const MC* in = reinterpret_cast<const MC*>(src) + ioff;
-        const MC ra = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MC{0, 0};
-        const MC rb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MC{0, 0};
-        A = mk(mkr<R>(ra.x, emax), mkr<R>(ra.y, emax));
-        B = mk(mkr<R>(rb.x, emax), mkr<R>(rb.y, emax));
+        A = mk(mkr<R>(ra[r].x, emax), mkr<R>(ra[r].y, emax));
+        B = mk(mkr<R>(rb[r].x, emax), mkr<R>(rb[r].y, emax));
       }
       if (k == 0 || 2 * k == M) { A.im = R(0); B.im = R(0); }
       // pos < m: A + iB ; else conj(A) + i conj(B): one formula with the
@@ -395,8 +423,8 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
           for (int r = 0; r < 8; ++r) {
             const Cx<R> y = apply_scale(v[r], a);
             MC o;
-            o.x = outr<R>(y.re, emax);
-            o.y = outr<R>(y.im, emax);
+            o.x = outr<R>(y.re, emax_out);
+            o.y = outr<R>(y.im, emax_out);
             out[(int64_t)(b + r * T) * a.out_sa] = o;
           }
         }
@@ -408,16 +436,19 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       for (int r = 0; r < 8; ++r) {
         const Cx<R> y = apply_scale(v[r], a);
         const int64_t off = (int64_t)(b + r * T) * a.out_sa;
-        if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax);
-        if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax);
+        if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax_out);
+        if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax_out);
       }
     }
     return;
   }
 
   // via shared memory: transposed layouts and the r2c split
+  {
+    Cx<R>* zw = z + sidx<R, LOGM>(p, b);
 #pragma unroll
-  for (int r = 0; r < 8; ++r) z[sidx<R, LOGM>(p, b + r * T)] = v[r];
+    for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * T)] = v[r];
+  }
   __syncthreads();
   const int nth = blockDim.x;
   if (a.op == OP_C2C) {
@@ -436,8 +467,8 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
       } else {
         MC o;
-        o.x = outr<R>(y.re, emax);
-        o.y = outr<R>(y.im, emax);
+        o.x = outr<R>(y.re, emax_out);
+        o.y = outr<R>(y.im, emax_out);
         out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = o;
       }
     }
@@ -462,14 +493,14 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       } else {
         if (i0 < nvalid) {
           MC o;
-          o.x = outr<R>(A.re, emax);
-          o.y = outr<R>(A.im, emax);
+          o.x = outr<R>(A.re, emax_out);
+          o.y = outr<R>(A.im, emax_out);
           out[off + (int64_t)i0 * a.out_st] = o;
         }
         if (i1 < nvalid) {
           MC o;
-          o.x = outr<R>(B.re, emax);
-          o.y = outr<R>(B.im, emax);
+          o.x = outr<R>(B.re, emax_out);
+          o.y = outr<R>(B.im, emax_out);
           out[off + (int64_t)i1 * a.out_st] = o;
         }
       }
@@ -483,8 +514,8 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       const Cx<R> y = apply_scale(z[sidx<R, LOGM>(q, k)], a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
-      if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax);
-      if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax);
+      if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax_out);
+      if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax_out);
     }
   }
 }

@@ -575,6 +575,14 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   const ld sc = 1.0L / (ld)P->scale;
   F.scale_h = (float)sc;
   F.scale_l = (float)(sc - (ld)F.scale_h);
+  if (F.scale_on && P->rb == 8 && !ps.out_dd) {
+    // a power-of-two normalisation of double outputs is an exponent offset
+    int k = 0;
+    if (frexpl(sc, &k) == 0.5L) {
+      F.scale_on = 0;
+      F.emax_shift = k - 1;
+    }
+  }
   F.deriv = A.deriv;
   F.deriv_role = A.deriv_role;
   F.deriv_half = A.deriv_half;
