@@ -80,13 +80,18 @@ typedef struct pfgb_plan_desc {
 } pfgb_plan_desc;
 
 /* Arithmetic of the transform kernels.
- *   DEFAULT: Float32 plans compute in FP32; Float64 plans compute power-of-two
- *            c2c/r2c/c2r lines in double-float (two FP32 values, 48-bit
- *            significand, on the FP32 pipes) and every other line in native
- *            FP64.  Both meet a relative L2 error of 1e-13.
- *   NATIVE:  Float64 plans compute every line in native FP64 (GB300's FP64
- *            rate is about 1/70 of its FP32 rate). */
-enum { PFGB_PRECISION_DEFAULT = 0, PFGB_PRECISION_NATIVE = 1 };
+ *   DEFAULT:  Float32 plans compute in FP32; Float64 plans compute power-of-two
+ *             c2c/r2c/c2r lines in double-float (two FP32 values, 48-bit
+ *             significand, on the FP32 pipes) and every other line in native
+ *             FP64.  Both meet a relative L2 error of 1e-13.
+ *   NATIVE:   Float64 plans compute every line in native FP64 (GB300's FP64
+ *             rate is about 1/70 of its FP32 rate).
+ *   TC_SPLIT: Float32 plans only: c2c lines of 256, 512 and 1024 points run
+ *             as two DFT-matrix products on the tensor cores (tf32 hi/lo
+ *             split, three products, FP32 accumulation); other lines as in
+ *             DEFAULT.  Relative L2 error about 1e-6 for a 3D round trip.
+ *             The benchmark spec's precision form; FFTW has no such mode. */
+enum { PFGB_PRECISION_DEFAULT = 0, PFGB_PRECISION_NATIVE = 1, PFGB_PRECISION_TC_SPLIT = 2 };
 
 typedef struct pfgb_plan pfgb_plan;
 
@@ -212,6 +217,14 @@ int pfgb_plan_get_timing(pfgb_plan* plan, pfgb_pass_timing* out, int max, int* n
  * capture.  All calls share the array: calls that overlap on the GPU race. */
 int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* out, const void* in,
                        void* stream);
+
+/* Device-side status of the plan's persistent kernels: synchronises `stream`,
+ * then returns in *flags, and clears, the bits set by bounded device waits
+ * that gave up since the last call (1: a TMA tile copy of fast_pass_tma,
+ * 2: a tensor-core product of tc_pass; the kernel then skipped the rest of
+ * its tiles).  No counterpart in the reference: FFTW calls cannot stall on
+ * a device. */
+int pfgb_device_status(pfgb_plan* plan, void* stream, int32_t* flags);
 
 /* Copies the message of the last failure on this thread into buf. Returns the
  * message length. */

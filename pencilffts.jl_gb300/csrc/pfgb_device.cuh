@@ -421,7 +421,7 @@ __device__ __forceinline__ Cx<R> r2r_post(const Cx<R>* zl, const PassArgs& a, in
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
   const int nth = blockDim.x;
   const int tid = threadIdx.x;

@@ -58,10 +58,13 @@ struct FastArgs {
   int deriv, deriv_role, deriv_half;
   int64_t deriv_n;  // physical length of the dimension (frequency wrap)
   float k0_h, k0_l;
-  // persistent TMA form (fast_pass_tma): tiles of the pass and an error word
-  // set when a wait for a tile's copies gives up
+  // persistent forms (fast_pass_tma, tc_pass): tiles of the pass and an error
+  // word set when a bounded wait gives up
   int64_t total;
   int* err;
+  // tensor-core split form: the DFT matrices' tf32 hi / lo parts in the
+  // shared-memory operand layout (tc_pass)
+  const void* tcb;
 };
 
 // i k y for the frequency of index idx (fftfreq: idx - n above (n-1)/2,
@@ -281,6 +284,32 @@ __host__ __device__ constexpr int fast_min_blocks(int logm) {
                                       : 512 / fast_threads<R>(logm);
 }
 
+// Origin of tile `bid` (< 2^31) of a pass: first line t0 along the tile
+// dimension, element offsets of the tile in the pass input and output, and
+// the index along the derivative dimension when that is an outer one.  The
+// divisions are multiply-and-shift pairs prepared on the host.
+struct TileOrigin {
+  int64_t t0, ioff, ooff, didx;
+};
+__device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bid, int lines) {
+  unsigned rest = div31(bid, a.div_tiles);
+  const unsigned tile = bid - rest * (unsigned)a.ntiles;
+  TileOrigin o;
+  o.t0 = (int64_t)tile * lines;
+  o.ioff = o.t0 * a.in_st;
+  o.ooff = o.t0 * a.out_st;
+  o.didx = 0;
+  for (int d = 0; d < a.nouter; ++d) {
+    const unsigned q = div31(rest, a.div_osz[d]);
+    const int64_t idx = rest - q * (unsigned)a.osz[d];
+    rest = q;
+    o.ioff += idx * a.in_so[d];
+    o.ooff += idx * a.out_so[d];
+    if (a.deriv && a.deriv_role == 2 + d) o.didx = idx;
+  }
+  return o;
+}
+
 // One tile of a pass: load (from `src`: the pass input in global memory, or
 // a copy of the tile's input lines in shared memory), stages, store.  `src`
 // is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
@@ -299,22 +328,11 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   int p, b;
   if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
 
-  // tile decode (bid < 2^31: multiply-and-shift divisions)
-  unsigned rest = div31((unsigned)bid, a.div_tiles);
-  const unsigned tile = (unsigned)bid - rest * (unsigned)a.ntiles;
   const bool packed = a.op != OP_C2C;
   const int lines = packed ? 2 * TW : TW;
-  const int64_t t0 = (int64_t)tile * lines;
-  int64_t ioff = t0 * a.in_st, ooff = t0 * a.out_st;
-  int64_t didx = 0;  // index along the derivative dimension when it is an outer one
-  for (int d = 0; d < a.nouter; ++d) {
-    const unsigned q = div31(rest, a.div_osz[d]);
-    const int64_t idx = rest - q * (unsigned)a.osz[d];
-    rest = q;
-    ioff += idx * a.in_so[d];
-    ooff += idx * a.out_so[d];
-    if (a.deriv && a.deriv_role == 2 + d) didx = idx;
-  }
+  const TileOrigin o = tile_origin(a, (unsigned)bid, lines);
+  const int64_t t0 = o.t0, ooff = o.ooff, didx = o.didx;
+  int64_t ioff = o.ioff;
   const int nvalid = (int)min((int64_t)lines, a.nt - t0);
   if (soff >= 0) ioff = soff;
 
@@ -522,7 +540,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
 
 template <typename R, int LOGM, int SIGN>
 __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM)) fast_pass(const FastArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   fast_tile<R, LOGM, SIGN>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
 }
 

@@ -23,6 +23,7 @@
 #include "pencilfft_gb300.h"
 #include "pfgb_device.cuh"
 #include "pfgb_fast.cuh"
+#include "pfgb_tc.cuh"
 
 namespace pfgb {
 
@@ -110,6 +111,9 @@ struct Pass {
   bool in_dd = false, out_dd = false, reduce_before = false;
   int logm = 0;
   const void* ftw = nullptr;  // its twiddle table (float or dd entries)
+  // tensor-core split form (Float32 c2c, precision PFGB_PRECISION_TC_SPLIT)
+  bool tc = false;
+  const void* tcb = nullptr;  // DFT matrices, tf32 hi / lo in operand layout
   // launch geometry
   int lines = 1, clines = 1, bpl = 1, lp = 0, threads = 0;
   size_t smem = 0;
@@ -304,6 +308,63 @@ static int upload_fast_table(pfgb_plan* P, int M, const void** out) {
   return PFGB_OK;
 }
 
+// Geometry of the tensor-core split form (pfgb_tc.cu)
+int tc_lines(int logm);
+void tc_split_of(int logm, int& ln1, int& ln2);
+
+// DFT matrices of the tensor-core split form for lines of 2^logm points and
+// one sign: for each distinct factor N of the split, the real form
+// [[C, -S], [S, C]] of F_N[k][n] = exp(sign 2 pi i k n / N) (2N x 2N, rows
+// (re/im, k), columns (re/im, n)) as a tf32 hi part (round to nearest) and
+// the rounded remainder, each in the K-major operand layout of tc_pass.
+static int upload_tc_table(pfgb_plan* P, int logm, int sign, const void** out) {
+  if (P->query_only) {
+    *out = nullptr;
+    return PFGB_OK;
+  }
+  const std::string key = "tcb" + std::to_string(logm) + (sign < 0 ? "-" : "+");
+  auto it = P->tables.find(key);
+  if (it != P->tables.end()) {
+    *out = it->second;
+    return PFGB_OK;
+  }
+  auto tf32 = [](float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;  // nearest, ties away
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+  };
+  int ln1 = 0, ln2 = 0;
+  tc_split_of(logm, ln1, ln2);
+  std::vector<float> blob;
+  const int factors[2] = {1 << ln1, 1 << ln2};
+  for (int f = 0; f < (ln1 == ln2 ? 1 : 2); ++f) {
+    const int N = factors[f], K = 2 * N;
+    std::vector<float> hi((size_t)K * K), lo((size_t)K * K);
+    for (int row = 0; row < K; ++row)
+      for (int col = 0; col < K; ++col) {
+        const int c = row / N, k = row % N, c2 = col / N, m = col % N;
+        const std::complex<ld> w = expi_pi(2 * (int64_t)k * m, N);  // exp(-2 pi i k m / N)
+        const ld fr = w.real(), fi = sign < 0 ? w.imag() : -w.imag();
+        const ld v = c == 0 ? (c2 == 0 ? fr : -fi) : (c2 == 0 ? fi : fr);
+        const float h = tf32((float)v);
+        const size_t at = (size_t)tc_off(row, col, K) / 4;
+        hi[at] = h;
+        lo[at] = tf32((float)(v - (ld)h));
+      }
+    blob.insert(blob.end(), hi.begin(), hi.end());
+    blob.insert(blob.end(), lo.begin(), lo.end());
+  }
+  void* d = nullptr;
+  PFGB_CUDA(cudaMalloc(&d, blob.size() * sizeof(float)));
+  PFGB_CUDA(cudaMemcpy(d, blob.data(), blob.size() * sizeof(float), cudaMemcpyHostToDevice));
+  P->tables[key] = d;
+  *out = d;
+  return PFGB_OK;
+}
+
 // Radix plan for a DFT length: returns false if a prime factor > 13 remains.
 static bool factor_radices(int n, std::vector<int>& rad) {
   rad.clear();
@@ -431,6 +492,12 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
     ps.lines = packed ? 2 * ps.clines : ps.clines;
     ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm) : fast_threads<float>(ps.logm);
     ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm) : fast_smem<float>(ps.logm);
+    if (P->precision == PFGB_PRECISION_TC_SPLIT && ps.op == OP_C2C && tc_lines(ps.logm) > 0) {
+      ps.tc = true;
+      ps.clines = ps.lines = tc_lines(ps.logm);
+      rc = upload_tc_table(P, ps.logm, ps.sign, &ps.tcb);
+      if (rc) return rc;
+    }
     return PFGB_OK;
   }
   const int Lc = ps.L > 0 ? ps.L : ps.M;
@@ -633,6 +700,7 @@ int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStr
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_emax(const void* x, int64_t n, int* out, cudaStream_t s);
 int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
+int launch_tc(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
 
 #ifndef PFGB_FAST_TMA
@@ -938,7 +1006,12 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       int64_t grid = 0;
       int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr);
       if (rc) return rc;
-      if (tma_eligible(P, ps, F)) {
+      if (ps.tc) {
+        F.total = grid;
+        F.err = P->emax_dev + 1;
+        F.tcb = ps.tcb;
+        rc = launch_tc(ps.logm, ps.sign, F, s);
+      } else if (tma_eligible(P, ps, F)) {
         F.total = grid;
         F.err = P->emax_dev + 1;
         rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, s)
@@ -996,8 +1069,11 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
     return fail(PFGB_ERR_ARGUMENT, "too many extra_dims");
   if (d.real_bytes != 4 && d.real_bytes != 8)
     return fail(PFGB_ERR_ARGUMENT, "real type must be Float32 (4) or Float64 (8)");
-  if (d.precision_mode != PFGB_PRECISION_DEFAULT && d.precision_mode != PFGB_PRECISION_NATIVE)
-    return fail(PFGB_ERR_UNSUPPORTED, "precision mode not available in this build");
+  if (d.precision_mode != PFGB_PRECISION_DEFAULT && d.precision_mode != PFGB_PRECISION_NATIVE &&
+      d.precision_mode != PFGB_PRECISION_TC_SPLIT)
+    return fail(PFGB_ERR_ARGUMENT, "unknown precision mode");
+  if (d.precision_mode == PFGB_PRECISION_TC_SPLIT && d.real_bytes != 4)
+    return fail(PFGB_ERR_ARGUMENT, "the tensor-core split form applies to Float32 plans");
   for (int n = 0; n < d.ndims; ++n) {
     if (d.dims[n] < 1) return fail(PFGB_ERR_ARGUMENT, "dimensions must be positive");
     if (d.kind[n] < PFGB_FFT || d.kind[n] > PFGB_NOTRANSFORM)
@@ -1111,6 +1187,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
           if (!rc && PFGB_FAST_TMA)
             rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
                             : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);
+          if (!rc && ps.tc) rc = launch_tc(ps.logm, ps.sign, F, nullptr);
         } else {
           PassArgs A;
           std::memset(&A, 0, sizeof(A));
@@ -1188,6 +1265,20 @@ int pfgb_plan_set_timing(pfgb_plan* P, int on) {
   return PFGB_OK;
 }
 
+int pfgb_device_status(pfgb_plan* P, void* stream, int32_t* flags) {
+  if (!P || !flags) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  *flags = 0;
+  if (P->query_only || !P->emax_dev) return PFGB_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int word = 0;
+  PFGB_CUDA(cudaMemcpyAsync(&word, P->emax_dev + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PFGB_CUDA(cudaStreamSynchronize(s));
+  PFGB_CUDA(cudaMemsetAsync(P->emax_dev + 1, 0, sizeof(int), s));
+  PFGB_CUDA(cudaStreamSynchronize(s));
+  *flags = word;
+  return PFGB_OK;
+}
+
 int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
   if (!P || !n || (max > 0 && !out)) return fail(PFGB_ERR_ARGUMENT, "null argument");
   std::vector<pfgb_pass_timing> acc;
@@ -1204,6 +1295,7 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     e.op = red ? -2 : ps.pk == PK_COPY ? -1 : ps.op;
     e.bytes_per_launch = red ? ps.lin.bytes() : ps.lin.bytes() + ps.lout.bytes();
     const char* kname = red ? "emax_kernel" : ps.pk == PK_COPY ? "copy_kernel"
+                        : ps.tc ? "tc_pass<tf32x3>"
                         : ps.fast ? (P->rb == 8 ? "fast_pass<dd>" : "fast_pass<float>")
                                   : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);

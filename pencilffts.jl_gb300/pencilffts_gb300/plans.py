@@ -180,7 +180,7 @@ def _expand(transforms, N):
     return transforms
 
 
-PRECISION = {"default": 0, "native": 1}
+PRECISION = {"default": 0, "native": 1, "tc": 2}
 
 
 def _descriptor(dims, transforms, real_type, permute_dims, extra_dims, precision="default") -> PlanDesc:
@@ -230,9 +230,11 @@ class PencilFFTPlan:
     ``PencilFFTPlan(dims_global, transforms, real_type=float64; permute_dims,
     extra_dims)`` mirrors the reference constructor ``src/plans.jl:306-320``;
     ``proc_dims`` must be all ones (one GPU, no MPI).  ``precision`` selects
-    the kernel arithmetic of Float64 plans: "default" (double-float on the
-    FP32 pipes for power-of-two lines, FP64 elsewhere) or "native" (FP64
-    everywhere).  FFTW planning keywords
+    the kernel arithmetic: "default" (Float64 plans: double-float on the FP32
+    pipes for power-of-two lines, FP64 elsewhere), "native" (Float64 plans:
+    FP64 everywhere) or "tc" (Float32 plans: c2c lines of 256, 512 and 1024
+    points as tensor-core DFT-matrix products with a tf32 hi/lo split; rel. L2
+    about 1e-6).  FFTW planning keywords
     (``fftw_flags``, ``fftw_timelimit``) and ``transpose_method`` are accepted
     and ignored, as the reference does for GPU arrays (src/plans.jl:325-332).
     """
@@ -328,6 +330,15 @@ class PencilFFTPlan:
     # -- per-pass timing (reference: TimerOutputs sections) -----------------
     def set_timing(self, on: bool = True):
         _lib.check(self._L.pfgb_plan_set_timing(self._handle, 1 if on else 0), "pfgb_plan_set_timing")
+
+    def device_status(self):
+        """Bits set by bounded device waits that gave up since the last call
+        (1: TMA tile copy, 2: tensor-core product); synchronises the plan's
+        stream and clears them."""
+        flags = ctypes.c_int32(0)
+        _lib.check(self._L.pfgb_device_status(self._handle, self._stream_ptr(), ctypes.byref(flags)),
+                   "pfgb_device_status")
+        return flags.value
 
     def get_timing(self):
         """Per-pass event timings recorded since the last call (synchronises)."""

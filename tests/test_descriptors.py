@@ -167,3 +167,12 @@ def test_input_data_type():
     """reference test/transforms.jl:362-379."""
     assert P.plan_query((8, 6), (T.NoTransform(), T.FFT()), np.float32).eltype_in_complex
     assert not P.plan_query((8, 6), (T.NoTransform(), T.NoTransform()), np.float32).eltype_in_complex
+
+
+def test_tc_split_precision_descriptor():
+    """The tensor-core split form is a Float32-only precision mode."""
+    P.plan_query((64, 512, 256), T.FFT(), np.float32, precision="tc")
+    with pytest.raises(P.ArgumentError, match="Float32"):
+        P.plan_query((64, 512, 256), T.FFT(), np.float64, precision="tc")
+    with pytest.raises(P.ArgumentError, match="precision"):
+        P.plan_query((8, 8), T.FFT(), np.float32, precision="bf16")
