@@ -2,6 +2,8 @@
 // Float32 c2c lines of 256, 512 and 1024 points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pencilfft_gb300.h"
 #include "pfgb_tc.cuh"
 
@@ -19,12 +21,25 @@ static int launch_tc_one(const FastArgs& A, cudaStream_t s) {
   int dev = 0;
   cudaGetDevice(&dev);
   if (max_grid[dev] == 0) {
-    int sms = 0, per_sm = 0;
+    // resident CTAs per SM from the SM's shared memory, registers and tensor
+    // memory (the occupancy query, without a carveout preference, reported
+    // one CTA where the launch fits two)
+    cudaError_t e = cudaFuncSetAttribute(tc_pass<LN1, LN2, SIGN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(carveout)");
+    int sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_pass<LN1, LN2, SIGN>, 256, C::SMEM);
-    if (e != cudaSuccess) return fail_cuda(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    const int by_tmem = 512 / C::TMEM_COLS;  // tensor memory: 512 columns per SM
-    if (per_sm > by_tmem) per_sm = by_tmem;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, tc_pass<LN1, LN2, SIGN>);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaFuncGetAttributes(tc_pass)");
+    const int regs = (fa.numRegs + 7) / 8 * 8;
+    int per_sm = smem_sm / (C::SMEM + reserved);
+    per_sm = std::min(per_sm, regs_sm / (regs * 256));
+    per_sm = std::min(per_sm, 512 / C::TMEM_COLS);  // tensor memory: 512 columns per SM
+    per_sm = std::min(per_sm, 2048 / 256);
     max_grid[dev] = sms * (per_sm > 0 ? per_sm : 1);
   }
   if (A.total == 0) return PFGB_OK;

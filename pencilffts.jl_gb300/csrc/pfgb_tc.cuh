@@ -26,9 +26,10 @@
 // axis-contiguous and the strided layouts and the transposed stage-2 writes
 // of a warp fill one core matrix (32 distinct banks).
 //
-// CTAs of 256 threads, persistent over the tiles of the pass: the DFT
-// matrices (hi / lo) and the twiddle table are copied into shared memory
-// once.  Thread 0 issues the MMAs and commits them to an mbarrier; waits are
+// CTAs of 256 threads (two per SM), persistent over the tiles of the pass:
+// the DFT matrices (hi / lo) and the twiddle table are copied into shared
+// memory once, and a tile's inputs are loaded into registers while the
+// previous tile's second product runs.  Thread 0 issues the MMAs and commits them to an mbarrier; waits are
 // bounded (error word, then the tensor memory is released).
 #pragma once
 
@@ -216,19 +217,29 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
   unsigned phase = 0;
   int failed = 0;
 
-  for (int64_t bid = blockIdx.x; bid < a.total; bid += gridDim.x) {
-    const TileOrigin o = tile_origin(a, (unsigned)bid, L);
-    const int nvalid = (int)min((int64_t)L, a.nt - o.t0);
-
-    // ---- stage-1 operand: x[line][N2 n1 + n2], n1 in this thread's range ----
-    {
-      const float2* in = reinterpret_cast<const float2*>(a.in) + o.ioff + (int64_t)line1 * a.in_st;
-      float2 x[NP1];
+  // inputs x[line][N2 n1 + n2] of a tile, n1 in this thread's range; the
+  // next tile's are loaded while the current tile's second product runs
+  float2 x[NP1];
+  TileOrigin onext;
+  int nvnext = 0;
+  auto load_tile = [&](int64_t b) {
+    onext = tile_origin(a, (unsigned)b, L);
+    nvnext = (int)min((int64_t)L, a.nt - onext.t0);
+    const float2* in = reinterpret_cast<const float2*>(a.in) + onext.ioff + (int64_t)line1 * a.in_st;
 #pragma unroll
-      for (int j = 0; j < NP1; ++j) {
-        const int n1 = q1 * NP1 + j;
-        x[j] = line1 < nvalid ? in[(int64_t)(n1 * N2 + n2) * a.in_sa] : zero2;
-      }
+    for (int j = 0; j < NP1; ++j) {
+      const int n1 = q1 * NP1 + j;
+      x[j] = line1 < nvnext ? in[(int64_t)(n1 * N2 + n2) * a.in_sa] : zero2;
+    }
+  };
+  if ((int64_t)blockIdx.x < a.total) load_tile(blockIdx.x);
+
+  for (int64_t bid = blockIdx.x; bid < a.total; bid += gridDim.x) {
+    const TileOrigin o = onext;
+    const int nvalid = nvnext;
+
+    // ---- stage-1 operand ----
+    {
       if (a.deriv == 1) {
 #pragma unroll
         for (int j = 0; j < NP1; ++j) {
@@ -311,6 +322,7 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
           }
       tc_commit(bar);
     }
+    if (bid + gridDim.x < a.total) load_tile(bid + gridDim.x);
     if (!mbar_wait_bounded(bar, phase)) failed = 1;
     phase ^= 1;
     tc_fence_after();
