@@ -29,8 +29,10 @@
 // CTAs of 256 threads (two per SM), persistent over the tiles of the pass:
 // the DFT matrices (hi / lo) and the twiddle table are copied into shared
 // memory once, and a tile's inputs are loaded into registers while the
-// previous tile's second product runs.  Thread 0 issues the MMAs and commits them to an mbarrier; waits are
-// bounded (error word, then the tensor memory is released).
+// previous tile's second product runs.  Thread 0 issues the MMAs, commits
+// them to an mbarrier and alone polls it (bounded: error word, then the
+// tensor memory is released); the other warps wait at the CTA barrier, which
+// costs no issue slots.
 #pragma once
 
 #include "pfgb_fast.cuh"
@@ -97,10 +99,16 @@ __device__ __forceinline__ void tc_commit(unsigned long long* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// x rounded to tf32 (10 explicit significand bits), to nearest with ties
+// away from zero, as two integer operations on the bit pattern (finite x)
 __device__ __forceinline__ float tf32_rn(float x) {
+#ifdef PFGB_TC_CVT
   unsigned r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
+#else
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+#endif
 }
 
 // Two 32-lane x N-column loads from tensor memory and the wait for them in
@@ -202,10 +210,16 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
   const unsigned tmem = *tslot;
   const unsigned lanes = (unsigned)((warp & 3) * 32) << 16;  // this warp's TMEM lane quarter
 
+  // operand descriptors at the operands' first byte; an MMA adds its byte
+  // offset / 16 to the start-address field (addresses stay below 2^18)
   const unsigned sA[2] = {smem_u32(Ahi), smem_u32(Alo)};
   const unsigned sB1[2] = {smem_u32(Bs), smem_u32(Bs + C::B1BYTES)};
   const unsigned sB2[2] = {C::B2BYTES ? smem_u32(Bs + 2 * C::B1BYTES) : sB1[0],
                            C::B2BYTES ? smem_u32(Bs + 2 * C::B1BYTES + C::B2BYTES) : sB1[1]};
+  const unsigned long long dA1[2] = {tc_sdesc(sA[0], 128, SBO1), tc_sdesc(sA[1], 128, SBO1)};
+  const unsigned long long dA2[2] = {tc_sdesc(sA[0], 128, SBO2), tc_sdesc(sA[1], 128, SBO2)};
+  const unsigned long long dB1[2] = {tc_sdesc(sB1[0], 128, SBO1), tc_sdesc(sB1[1], 128, SBO1)};
+  const unsigned long long dB2[2] = {tc_sdesc(sB2[0], 128, SBO2), tc_sdesc(sB2[1], 128, SBO2)};
 
   // thread roles: stage-1 row r1 = n2 L + line (part q1 of the row's n1 / k1
   // range), stage-2 row r2 = k1 L + line (part q2 of the row's k2 range)
@@ -215,7 +229,6 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
   const int k1o = r2 / L, line2 = r2 % L;
   const float2 zero2 = make_float2(0.f, 0.f);
   unsigned phase = 0;
-  int failed = 0;
 
   // inputs x[line][N2 n1 + n2] of a tile, n1 in this thread's range; the
   // next tile's are loaded while the current tile's second product runs
@@ -275,15 +288,15 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
 #pragma unroll
         for (int pr = 0; pr < 3; ++pr)  // hi*lo, lo*hi, then hi*hi
 #pragma unroll
-          for (int kk = 0; kk < C::K1 / 8; ++kk) {
-            const unsigned long long ad = tc_sdesc(sA[pr == 1] + b * 16 * SBO1 + kk * 256, 128, SBO1);
-            const unsigned long long bd = tc_sdesc(sB1[pr == 0] + kk * 256, 128, SBO1);
-            tc_mma(tmem + b * C::K1, ad, bd, ID1, (pr | kk) ? 1u : 0u);
-          }
+          for (int kk = 0; kk < C::K1 / 8; ++kk)
+            tc_mma(tmem + b * C::K1, dA1[pr == 1] + ((b * 16 * SBO1 + kk * 256) >> 4),
+                   dB1[pr == 0] + ((kk * 256) >> 4), ID1, (pr | kk) ? 1u : 0u);
       tc_commit(bar);
+      if (!mbar_wait_bounded(bar, phase)) *sfail = 1;
+      tc_fence_before();
     }
-    if (!mbar_wait_bounded(bar, phase)) failed = 1;
     phase ^= 1;
+    __syncthreads();
     tc_fence_after();
 
     // ---- twiddles, stage-2 operand: rows (k1, line), K = [re(n2) | im(n2)] ----
@@ -315,16 +328,18 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
 #pragma unroll
         for (int pr = 0; pr < 3; ++pr)
 #pragma unroll
-          for (int kk = 0; kk < C::K2 / 8; ++kk) {
-            const unsigned long long ad = tc_sdesc(sA[pr == 1] + b * 16 * SBO2 + kk * 256, 128, SBO2);
-            const unsigned long long bd = tc_sdesc(sB2[pr == 0] + kk * 256, 128, SBO2);
-            tc_mma(tmem + b * C::K2, ad, bd, ID2, (pr | kk) ? 1u : 0u);
-          }
+          for (int kk = 0; kk < C::K2 / 8; ++kk)
+            tc_mma(tmem + b * C::K2, dA2[pr == 1] + ((b * 16 * SBO2 + kk * 256) >> 4),
+                   dB2[pr == 0] + ((kk * 256) >> 4), ID2, (pr | kk) ? 1u : 0u);
       tc_commit(bar);
     }
     if (bid + gridDim.x < a.total) load_tile(bid + gridDim.x);
-    if (!mbar_wait_bounded(bar, phase)) failed = 1;
+    if (tid == 0) {
+      if (!mbar_wait_bounded(bar, phase)) *sfail = 1;
+      tc_fence_before();
+    }
     phase ^= 1;
+    __syncthreads();
     tc_fence_after();
 
     // ---- output X[line][k1 + N1 k2] ----
@@ -348,7 +363,6 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
       }
     }
     tc_fence_before();
-    if (failed) *sfail = 1;
     __syncthreads();
     if (*sfail) break;
   }
