@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--precision", default="default", choices=["default", "native", "tc"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the Float32 plain vs tensor-core split comparison")
     ap.add_argument("--cpu-sample-s", type=float, default=20.0,
                     help="approximate CPU seconds for the cpu_baseline sample")
     return ap.parse_args()
@@ -162,6 +164,60 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# Float32 forms: plain path against the tensor-core split form
+# ---------------------------------------------------------------------------
+def measure_forms(P, dims, steps, warmup, dev):
+    """Times the Float32 RFFT round trip of the same workload with the plain
+    kernels and with the tensor-core split form (precision="tc"), and states
+    each form's error: rel. L2 of the forward spectrum against the Float64
+    plan's spectrum (the double-float path, parity-tested against the FP64
+    oracle at 1e-13) and of the round trip against the input."""
+    import numpy as np
+    import torch
+
+    T = P.Transforms
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    p64 = P.PencilFFTPlan(dims, T.RFFT(), np.float64)
+    u64 = p64.allocate_input()
+    u64.data.uniform_(-1.0, 1.0, generator=g)
+    ref = p64 * u64
+    ref_norm = torch.linalg.vector_norm(ref.data).item()
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, prec in (("f32_plain", "default"), ("f32_tc_split", "tc")):
+        p = P.PencilFFTPlan(dims, T.RFFT(), np.float32, precision=prec)
+        u, v, w = p.allocate_input(), p.allocate_output(), p.allocate_input()
+        u.data.copy_(u64.data)
+        P.mul_(v, p, u)
+        e_fwd = (torch.linalg.vector_norm(v.data.to(ref.data.dtype) - ref.data).item() / ref_norm)
+        P.ldiv_(w, p, v)
+        e_rt = (torch.linalg.vector_norm(w.data - u.data).item() / torch.linalg.vector_norm(u.data).item())
+        for _ in range(warmup):
+            P.mul_(v, p, u)
+            P.ldiv_(w, p, v)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            P.mul_(v, p, u)
+            P.ldiv_(w, p, v)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"value": e0.elapsed_time(e1) / steps, "unit": UNIT,
+                     "rel_l2_forward": e_fwd, "rel_l2_round_trip": e_rt}
+        del p, u, v, w
+        torch.cuda.empty_cache()
+    out["tc_split_speedup_vs_plain"] = out["f32_plain"]["value"] / out["f32_tc_split"]["value"]
+    out["error_reference"] = ("forward: Float64 plan on the same input (double-float path, "
+                              "parity-tested against the FP64 oracle at 1e-13); round trip: the input")
+    del p64, u64, ref
+    torch.cuda.empty_cache()
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -317,6 +373,9 @@ def run_gpu(args, rank, world, local_rank):
 
     if rank != 0:
         return
+    forms = None
+    if not args.no_forms:
+        forms = measure_forms(P, dims, args.steps, args.warmup, dev)
     line = {
         "metric": METRIC, "value": ms_step, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -340,6 +399,7 @@ def run_gpu(args, rank, world, local_rank):
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
         "gpu_launches": launches,
+        "forms": forms,
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
