@@ -174,8 +174,27 @@ __device__ __forceinline__ int sidx(int p, int pos) {
 // j < Ls and L = Ls (stage writes): a thread forms one base address and
 // reaches its 8 slots at compile-time offsets.
 
+// Barrier of a stage exchange.  Each thread reads and writes only its own
+// line's slots, so with lines along the thread index (line p = threads
+// p T .. p T + T - 1) the T threads of a line synchronise alone: a named
+// barrier per line (ids 1..lines, T a multiple of 32) or a warp barrier when
+// a warp holds whole lines.  With lines across the thread index (strided
+// axis, lanes along the tile dimension) every warp holds every line.
+template <typename R, int LOGM>
+__device__ __forceinline__ void line_sync(bool lanes_across_lines, int p) {
+  constexpr int T = (1 << LOGM) / 8;
+  if (lanes_across_lines || T == fast_threads<R>(LOGM)) {
+    __syncthreads();
+  } else if constexpr (T <= 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + p), "r"(T) : "memory");
+  }
+}
+
 template <typename R, int LOGM, int SIGN>
-__device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int b, const void* tw) {
+__device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int b, const void* tw,
+                                            bool lanes_across_lines) {
   constexpr int M = 1 << LOGM;
   constexpr int T = M / 8;
   constexpr int S8 = LOGM / 3;
@@ -224,11 +243,11 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       }
     }
     if (!last) {
-      __syncthreads();
+      line_sync<R, LOGM>(lanes_across_lines, p);
       const Cx<R>* zr = z + sidx<R, LOGM>(p, b);
 #pragma unroll
       for (int r = 0; r < 8; ++r) v[r] = zr[padded<R, LOGM>(r * T)];
-      __syncthreads();
+      line_sync<R, LOGM>(lanes_across_lines, p);
     }
   }
 }
@@ -418,7 +437,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   }
 
   // ---- stages ----
-  fast_stages<R, LOGM, SIGN>(v, z, p, b, a.tw);
+  fast_stages<R, LOGM, SIGN>(v, z, p, b, a.tw, a.lmap_tile != 0);
 
   // ---- store ----
   if (a.deriv == 2 && a.store_direct && a.op == OP_C2C) {
