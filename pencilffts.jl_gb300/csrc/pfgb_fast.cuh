@@ -40,9 +40,20 @@ struct FastArgs {
   // the run's double input (computed by emax_kernel before the run).
   int in_dd, out_dd;
   const int* emax_ptr;
-  // added to *emax_ptr for the double outputs of the pass: the ldiv!
+  // added to the run exponent for the double outputs of the pass: the ldiv!
   // normalisation when it is a power of two (scale_on is then 0)
   int emax_shift;
+  // Run exponent without a separate reduction: the first pass of a run
+  // (self_scale) scales each tile by its own largest exponent, stores it in
+  // te[tile] and folds it into *emax_ptr (atomicMax; zeroed before the run);
+  // the second pass (te_rescale) multiplies each loaded element by
+  // 2^(te[tile1] - *emax_ptr), tile1 = sum over its roles (axis, tile
+  // dimension, outer dimension o) of (coordinate >> te_sh) * te_mul, the
+  // first pass's tile of that element.  Later passes use *emax_ptr.
+  int self_scale, te_rescale;
+  int* te;
+  int te_sh[2 + kMaxOuter];
+  unsigned te_mul[2 + kMaxOuter];
   int nouter;
   int64_t nt, ntiles;
   int64_t in_sa, in_st, out_sa, out_st;
@@ -309,6 +320,7 @@ __host__ __device__ constexpr int fast_min_blocks(int logm) {
 // divisions are multiply-and-shift pairs prepared on the host.
 struct TileOrigin {
   int64_t t0, ioff, ooff, didx;
+  unsigned tebase;  // te_rescale: the outer dimensions' part of the first-pass tile index
 };
 __device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bid, int lines) {
   unsigned rest = div31(bid, a.div_tiles);
@@ -318,6 +330,7 @@ __device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bi
   o.ioff = o.t0 * a.in_st;
   o.ooff = o.t0 * a.out_st;
   o.didx = 0;
+  o.tebase = 0;
   for (int d = 0; d < a.nouter; ++d) {
     const unsigned q = div31(rest, a.div_osz[d]);
     const int64_t idx = rest - q * (unsigned)a.osz[d];
@@ -325,8 +338,44 @@ __device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bi
     o.ioff += idx * a.in_so[d];
     o.ooff += idx * a.out_so[d];
     if (a.deriv && a.deriv_role == 2 + d) o.didx = idx;
+    o.tebase += ((unsigned)idx >> a.te_sh[2 + d]) * a.te_mul[2 + d];
   }
   return o;
+}
+
+// Largest biased exponent over the tile (self_scale): every thread passes
+// its own maximum; thread 0 records it for the next pass and in the run's
+// exponent word.  Called by all threads of the CTA.
+__device__ __forceinline__ int tile_exponent(unsigned emx, const FastArgs& a, unsigned bid) {
+  __shared__ unsigned wmax[32];
+  emx = __reduce_max_sync(0xFFFFFFFFu, emx);
+  const int nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = emx;
+  __syncthreads();
+  unsigned e = 0;
+  for (int w = 0; w < nw; ++w) e = max(e, wmax[w]);
+  if (threadIdx.x == 0) {
+    if (a.te) a.te[bid] = (int)e;
+    atomicMax(const_cast<int*>(a.emax_ptr), (int)e);
+  }
+  __syncthreads();  // wmax may be reused by the next tile of a persistent CTA
+  return (int)e;
+}
+__device__ __forceinline__ unsigned dexp_u(double x) {
+  return (unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu;
+}
+// 2^(te[tile1] - run exponent) for the element at axis coordinate pos of the
+// line at coordinate line along the tile dimension (te_rescale)
+__device__ __forceinline__ float te_factor(const FastArgs& a, unsigned tebase, int64_t line, int pos, int erun) {
+  const unsigned t1 = tebase + ((unsigned)line >> a.te_sh[1]) * a.te_mul[1] +
+                      ((unsigned)pos >> a.te_sh[0]) * a.te_mul[0];
+  const int d = __ldg(a.te + t1) - erun;
+  return d >= -126 ? __uint_as_float((unsigned)(d + 127) << 23) : 0.0f;
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> scale_pow2(Cx<R> y, float f) {
+  if constexpr (std::is_same<R, dd>::value) return mk(dd(y.re.h * f, y.re.l * f), dd(y.im.h * f, y.im.l * f));
+  else return mk(y.re * f, y.im * f);
 }
 
 // One tile of a pass: load (from `src`: the pass input in global memory, or
@@ -359,8 +408,10 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   Cx<R> v[8];
   int emax = 0, emax_out = 0;
   if constexpr (IO::kDD) {
-    emax = *a.emax_ptr;
-    emax_out = emax + a.emax_shift;
+    if (!a.self_scale) {
+      emax = *a.emax_ptr;
+      emax_out = emax + a.emax_shift;
+    }
   }
   if (a.op == OP_C2C) {
     if (IO::kDD && a.in_dd) {
@@ -370,6 +421,10 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         const float4 q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : make_float4(0.f, 0.f, 0.f, 0.f);
         v[r] = ld_dd4<R>(q);
       }
+      if (IO::kDD && a.te_rescale && p < nvalid) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = scale_pow2(v[r], te_factor(a, o.tebase, t0 + p, b + r * T, emax));
+      }
     } else {
       // all loads first, conversions after: the conversion's rare-case
       // branch must not serialise the loads
@@ -377,6 +432,15 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       MC raw[8];
 #pragma unroll
       for (int r = 0; r < 8; ++r) raw[r] = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
+          emax = tile_exponent(emx, a, (unsigned)bid);
+          emax_out = emax + a.emax_shift;
+        }
+      }
 #pragma unroll
       for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
     }
@@ -397,6 +461,15 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MR(0);
       rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MR(0);
     }
+    if constexpr (IO::kDD) {
+      if (a.self_scale) {
+        unsigned emx = 0;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
+        emax = tile_exponent(emx, a, (unsigned)bid);
+        emax_out = emax + a.emax_shift;
+      }
+    }
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
   } else {  // OP_C2R: Hermitian extension of two half spectra, n = M, m = n_in
@@ -412,6 +485,16 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MC{0, 0};
         rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MC{0, 0};
       }
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < 8; ++r)
+            emx = max(emx, max(max(dexp_u(ra[r].x), dexp_u(ra[r].y)), max(dexp_u(rb[r].x), dexp_u(rb[r].y))));
+          emax = tile_exponent(emx, a, (unsigned)bid);
+          emax_out = emax + a.emax_shift;
+        }
+      }
     }
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -424,6 +507,10 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         A = ld_dd4<R>(i0 < nvalid ? in[off + (int64_t)i0 * sst] : z4);
         B = ld_dd4<R>(i1 < nvalid ? in[off + (int64_t)i1 * sst] : z4);
+        if (IO::kDD && a.te_rescale) {
+          if (i0 < nvalid) A = scale_pow2(A, te_factor(a, o.tebase, t0 + i0, k, emax));
+          if (i1 < nvalid) B = scale_pow2(B, te_factor(a, o.tebase, t0 + i1, k, emax));
+        }
       } else {
         A = mk(mkr<R>(ra[r].x, emax), mkr<R>(ra[r].y, emax));
         B = mk(mkr<R>(rb[r].x, emax), mkr<R>(rb[r].y, emax));

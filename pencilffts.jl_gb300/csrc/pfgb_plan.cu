@@ -109,6 +109,12 @@ struct Pass {
   // Float64 fast passes: dd-form input / output between consecutive dd passes,
   // and an exponent reduction over the input before the first pass of a run
   bool in_dd = false, out_dd = false, reduce_before = false;
+  // run exponent without a reduction pass: the first pass of a run scales
+  // each tile by itself (self_scale); the second maps each element to its
+  // first-pass tile (te_rescale, te_sh / te_mul per role)
+  bool self_scale = false, te_rescale = false;
+  int te_sh[2 + kMaxOuter] = {};
+  unsigned te_mul[2 + kMaxOuter] = {};
   int logm = 0;
   const void* ftw = nullptr;  // its twiddle table (float or dd entries)
   // tensor-core split form (Float32 c2c, precision PFGB_PRECISION_TC_SPLIT)
@@ -158,6 +164,7 @@ struct pfgb_plan {
   std::vector<void*> allocations;
   std::map<std::string, void*> tables;
   int* emax_dev = nullptr;  // scale exponent of the current run of dd passes
+  int* te_dev = nullptr;    // per-tile exponents of a run's first pass
   int device = 0;
   bool query_only = false;  // plan analysed on the host only (no device memory)
   // opt-in per-launch timing: (direction, pass index, start, stop)
@@ -530,6 +537,60 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
 }
 
 // Fills the kernel arguments of a transform pass for given buffers.
+// Tile dimension of a pass (-1 for 1D): the contiguous dimension of the
+// input when the axis is not, else the output's, else the next in the input.
+static int tile_dim(const Pass& ps) {
+  const int a = ps.axis;
+  const bool a_fast_in = ps.lin.perm[0] == a;
+  const bool a_fast_out = ps.lout.perm[0] == a;
+  if (!a_fast_in) return ps.lin.perm[0];
+  if (!a_fast_out) return ps.lout.perm[0];
+  return ps.lin.D > 1 ? ps.lin.perm[1] : -1;
+}
+
+// Element -> first-pass tile map of the second pass of a Float64 run: the
+// first pass p1 numbers its tiles (lines grouped by p1.lines along its tile
+// dimension t1) + ntiles1 * (outer index in p1's input order); for each role
+// of p2 (axis, tile dimension, outer dimensions in p2's input order) the
+// coordinate contributes (c >> sh) * mul.  Returns p1's number of tiles.
+static int64_t te_mapping(const Pass& p1, Pass& p2) {
+  const int a1 = p1.axis, t1 = tile_dim(p1);
+  int sh1 = 0;
+  while ((1 << sh1) < p1.lines) ++sh1;
+  const int64_t ntiles1 = t1 >= 0 ? (p1.lin.size[t1] + p1.lines - 1) / p1.lines : 1;
+  int64_t mul1[kMaxD] = {};
+  int64_t m = ntiles1;
+  for (int q = 0; q < p1.lin.D; ++q) {
+    const int d = p1.lin.perm[q];
+    if (d == a1 || d == t1) continue;
+    mul1[d] = m;
+    m *= p1.lin.size[d];
+  }
+  auto role = [&](int d, int& sh, unsigned& mul) {
+    if (d >= 0 && d == t1) {
+      sh = sh1;
+      mul = 1;
+    } else if (d < 0 || d == a1) {
+      sh = 0;
+      mul = 0;
+    } else {
+      sh = 0;
+      mul = (unsigned)mul1[d];
+    }
+  };
+  const int t2 = tile_dim(p2);
+  role(p2.axis, p2.te_sh[0], p2.te_mul[0]);
+  role(t2, p2.te_sh[1], p2.te_mul[1]);
+  int o = 0;
+  for (int q = 0; q < p2.lin.D && o < kMaxOuter; ++q) {
+    const int d = p2.lin.perm[q];
+    if (d == p2.axis || d == t2) continue;
+    role(d, p2.te_sh[2 + o], p2.te_mul[2 + o]);
+    ++o;
+  }
+  return m;
+}
+
 static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* out, bool scale_on,
                      PassArgs& A, int64_t& grid, const Deriv* dv = nullptr) {
   std::memset(&A, 0, sizeof(A));
@@ -638,6 +699,13 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.in_dd = ps.in_dd ? 1 : 0;
   F.out_dd = ps.out_dd ? 1 : 0;
   F.emax_ptr = P->emax_dev;
+  F.self_scale = ps.self_scale ? 1 : 0;
+  F.te_rescale = ps.te_rescale ? 1 : 0;
+  F.te = (ps.self_scale && ps.out_dd) || ps.te_rescale ? P->te_dev : nullptr;
+  for (int i = 0; i < 2 + kMaxOuter; ++i) {
+    F.te_sh[i] = ps.te_sh[i];
+    F.te_mul[i] = ps.te_mul[i];
+  }
   F.scale_on = scale_on ? 1 : 0;
   const ld sc = 1.0L / (ld)P->scale;
   F.scale_h = (float)sc;
@@ -977,18 +1045,8 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
     void* out = buf(ps.bout);
     if (ps.pk == PK_COPY && in == out && ps.lin.same_order(ps.lout)) continue;
     if (ps.fast && ps.reduce_before) {
-      pfgb_plan::Rec rr{dsign, 100 + i, nullptr, nullptr};
-      if (P->timing) {
-        PFGB_CUDA(cudaEventCreate(&rr.a));
-        PFGB_CUDA(cudaEventCreate(&rr.b));
-        PFGB_CUDA(cudaEventRecord(rr.a, s));
-      }
-      int rc = launch_emax(in, ps.lin.bytes() / 8, P->emax_dev, s);
-      if (rc) return rc;
-      if (P->timing) {
-        PFGB_CUDA(cudaEventRecord(rr.b, s));
-        P->recs.push_back(rr);
-      }
+      // the run's exponent word collects the first pass's tile exponents
+      PFGB_CUDA(cudaMemsetAsync(P->emax_dev, 0, sizeof(int), s));
     }
     pfgb_plan::Rec rec{dsign, i, nullptr, nullptr};
     if (P->timing) {
@@ -1197,6 +1255,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
     }
   }
   // Float64 runs of consecutive fast passes exchange data in dd form
+  int64_t te_tiles = 0;
   if (!rc && P->rb == 8) {
     for (auto* dir : {&P->fwd, &P->bwd}) {
       auto& v = dir->passes;
@@ -1207,8 +1266,18 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
         v[i].in_dd = prev;
         v[i].out_dd = next;
         v[i].reduce_before = !prev;
+        v[i].self_scale = !prev;
       }
+      for (size_t i = 0; i + 1 < v.size(); ++i)
+        if (v[i].self_scale && v[i].out_dd) {
+          v[i + 1].te_rescale = true;
+          te_tiles = std::max(te_tiles, te_mapping(v[i], v[i + 1]));
+        }
     }
+  }
+  if (!rc && !query_only && te_tiles > 0) {
+    cudaError_t e = cudaMalloc(&P->te_dev, (size_t)te_tiles * sizeof(int));
+    if (e != cudaSuccess) rc = fail(PFGB_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   }
   // exponent word (Float64 runs) and error word of the TMA-fed passes
   if (!rc && !query_only) {
@@ -1323,6 +1392,7 @@ int pfgb_plan_destroy(pfgb_plan* P) {
     if (P->scratch[s]) cudaFree(P->scratch[s]);
   for (auto& kv : P->tables) cudaFree(kv.second);
   if (P->emax_dev) cudaFree(P->emax_dev);
+  if (P->te_dev) cudaFree(P->te_dev);
   delete P;
   return PFGB_OK;
 }
