@@ -44,14 +44,17 @@ struct FastArgs {
   // normalisation when it is a power of two (scale_on is then 0)
   int emax_shift;
   // Run exponent without a separate reduction: the first pass of a run
-  // (self_scale) scales each tile by its own largest exponent, stores it in
-  // te[tile] and folds it into *emax_ptr (atomicMax; zeroed before the run);
-  // the second pass (te_rescale) multiplies each loaded element by
-  // 2^(te[tile1] - *emax_ptr), tile1 = sum over its roles (axis, tile
-  // dimension, outer dimension o) of (coordinate >> te_sh) * te_mul, the
-  // first pass's tile of that element.  Later passes use *emax_ptr.
+  // (self_scale) scales each complex line by its own largest exponent (the
+  // tile's, when lines lie across the thread index), stores it in te[line]
+  // (line = t0 / pk + p + te_ncl * outer index, pk = 2 real lines per
+  // complex line when packed) and folds it into *emax_ptr (atomicMax; zeroed
+  // before the run); the second pass (te_rescale) multiplies each loaded
+  // element by 2^(te[line1] - *emax_ptr), line1 = sum over its roles (axis,
+  // tile dimension, outer dimension o) of (coordinate >> te_sh) * te_mul, the
+  // first-pass line of that element.  Later passes use *emax_ptr.
   int self_scale, te_rescale;
   int* te;
+  int64_t te_ncl;
   int te_sh[2 + kMaxOuter];
   unsigned te_mul[2 + kMaxOuter];
   int nouter;
@@ -343,22 +346,50 @@ __device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bi
   return o;
 }
 
-// Largest biased exponent over the tile (self_scale): every thread passes
-// its own maximum; thread 0 records it for the next pass and in the run's
-// exponent word.  Called by all threads of the CTA.
-__device__ __forceinline__ int tile_exponent(unsigned emx, const FastArgs& a, unsigned bid) {
+// Scale exponent of the thread's complex line in the first pass of a run
+// (self_scale): the largest biased exponent over the line (over the tile when
+// lines lie across the thread index).  The lines' leaders record it for the
+// next pass and fold it into the run's exponent word.  Called by all threads.
+template <typename R, int LOGM>
+__device__ __forceinline__ int line_exponent(unsigned emx, const FastArgs& a, unsigned bid, int64_t t0,
+                                             int p, int nvalid_cl, bool lanes_across_lines) {
+  constexpr int T = (1 << LOGM) / 8;
+  constexpr int TW = fast_tw<R>(LOGM);
   __shared__ unsigned wmax[32];
-  emx = __reduce_max_sync(0xFFFFFFFFu, emx);
-  const int nw = (blockDim.x + 31) >> 5;
-  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = emx;
-  __syncthreads();
-  unsigned e = 0;
-  for (int w = 0; w < nw; ++w) e = max(e, wmax[w]);
-  if (threadIdx.x == 0) {
-    if (a.te) a.te[bid] = (int)e;
-    atomicMax(const_cast<int*>(a.emax_ptr), (int)e);
+  unsigned e;
+  bool leader;
+  if (lanes_across_lines || T == fast_threads<R>(LOGM)) {
+    emx = __reduce_max_sync(0xFFFFFFFFu, emx);
+    const int nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = emx;
+    __syncthreads();
+    e = 0;
+    for (int w = 0; w < nw; ++w) e = max(e, wmax[w]);
+    __syncthreads();  // wmax is reused by the next tile of a persistent CTA
+    leader = lanes_across_lines ? (int)threadIdx.x < TW : threadIdx.x == 0;
+  } else if constexpr (T <= 32) {
+    const unsigned mask = (T == 32 ? 0xFFFFFFFFu : ((1u << T) - 1u)) << ((p * T) & 31);
+    e = __reduce_max_sync(mask, emx);
+    leader = (threadIdx.x % T) == 0;
+  } else {
+    emx = __reduce_max_sync(0xFFFFFFFFu, emx);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = emx;
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + p), "r"(T) : "memory");
+    e = 0;
+#pragma unroll
+    for (int w = 0; w < T / 32; ++w) e = max(e, wmax[p * (T / 32) + w]);
+    leader = (threadIdx.x % T) == 0;
   }
-  __syncthreads();  // wmax may be reused by the next tile of a persistent CTA
+  // leader of line q: line p in the per-line branches, thread q in the
+  // tile-wide branch (all lines share e)
+  const int q = (lanes_across_lines && !(T == fast_threads<R>(LOGM))) ? (int)threadIdx.x
+                : (T == fast_threads<R>(LOGM) ? 0 : p);
+  if (leader && q < nvalid_cl) {
+    const int pk = a.op == OP_C2C ? 1 : 2;
+    const unsigned rest = div31(bid, a.div_tiles);
+    if (a.te) a.te[t0 / pk + q + a.te_ncl * rest] = (int)e;
+    if ((int)e > *reinterpret_cast<const volatile int*>(a.emax_ptr)) atomicMax(const_cast<int*>(a.emax_ptr), (int)e);
+  }
   return (int)e;
 }
 __device__ __forceinline__ unsigned dexp_u(double x) {
@@ -402,6 +433,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   const int64_t t0 = o.t0, ooff = o.ooff, didx = o.didx;
   int64_t ioff = o.ioff;
   const int nvalid = (int)min((int64_t)lines, a.nt - t0);
+  const int ncl_valid = packed ? (nvalid + 1) / 2 : nvalid;  // complex lines with data
   if (soff >= 0) ioff = soff;
 
   // ---- load: v[r] = line p, element b + r T (stage-1 Stockham inputs) ----
@@ -437,7 +469,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
           unsigned emx = 0;
 #pragma unroll
           for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
-          emax = tile_exponent(emx, a, (unsigned)bid);
+          emax = line_exponent<R, LOGM>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
@@ -466,7 +498,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         unsigned emx = 0;
 #pragma unroll
         for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
-        emax = tile_exponent(emx, a, (unsigned)bid);
+        emax = line_exponent<R, LOGM>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
         emax_out = emax + a.emax_shift;
       }
     }
@@ -491,7 +523,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
 #pragma unroll
           for (int r = 0; r < 8; ++r)
             emx = max(emx, max(max(dexp_u(ra[r].x), dexp_u(ra[r].y)), max(dexp_u(rb[r].x), dexp_u(rb[r].y))));
-          emax = tile_exponent(emx, a, (unsigned)bid);
+          emax = line_exponent<R, LOGM>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
@@ -522,6 +554,10 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       v[r] = mk(A.re - B.im, A.im + B.re);
     }
   }
+
+  // per-line exponents of a self-scaled pass, for the stores of other lines
+  __shared__ int lexp[TW];
+  if (IO::kDD && a.self_scale && b == 0) lexp[p] = emax;
 
   // ---- stages ----
   fast_stages<R, LOGM, SIGN>(v, z, p, b, a.tw, a.lmap_tile != 0);
@@ -575,6 +611,9 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   }
   __syncthreads();
   const int nth = blockDim.x;
+  // output exponent of complex line i (the first pass of a run scales lines
+  // separately; the loops below write other threads' lines)
+  auto line_emax_out = [&](int i) { return IO::kDD && a.self_scale ? lexp[i] + a.emax_shift : emax_out; };
   if (a.op == OP_C2C) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
     const int tot = TW * M;
@@ -590,9 +629,10 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       if (IO::kDD && a.out_dd) {
         reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
       } else {
+        const int eo = line_emax_out(i);
         MC o;
-        o.x = outr<R>(y.re, emax_out);
-        o.y = outr<R>(y.im, emax_out);
+        o.x = outr<R>(y.re, eo);
+        o.y = outr<R>(y.im, eo);
         out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = o;
       }
     }
@@ -615,16 +655,17 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         if (i0 < nvalid) o4[off + (int64_t)i0 * a.out_st] = st_dd4(A);
         if (i1 < nvalid) o4[off + (int64_t)i1 * a.out_st] = st_dd4(B);
       } else {
+        const int eo = line_emax_out(q);
         if (i0 < nvalid) {
           MC o;
-          o.x = outr<R>(A.re, emax_out);
-          o.y = outr<R>(A.im, emax_out);
+          o.x = outr<R>(A.re, eo);
+          o.y = outr<R>(A.im, eo);
           out[off + (int64_t)i0 * a.out_st] = o;
         }
         if (i1 < nvalid) {
           MC o;
-          o.x = outr<R>(B.re, emax_out);
-          o.y = outr<R>(B.im, emax_out);
+          o.x = outr<R>(B.re, eo);
+          o.y = outr<R>(B.im, eo);
           out[off + (int64_t)i1 * a.out_st] = o;
         }
       }
@@ -638,8 +679,9 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       const Cx<R> y = apply_scale(z[sidx<R, LOGM>(q, k)], a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
-      if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax_out);
-      if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax_out);
+      const int eo = line_emax_out(q);
+      if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, eo);
+      if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
     }
   }
 }

@@ -548,18 +548,26 @@ static int tile_dim(const Pass& ps) {
   return ps.lin.D > 1 ? ps.lin.perm[1] : -1;
 }
 
-// Element -> first-pass tile map of the second pass of a Float64 run: the
-// first pass p1 numbers its tiles (lines grouped by p1.lines along its tile
-// dimension t1) + ntiles1 * (outer index in p1's input order); for each role
-// of p2 (axis, tile dimension, outer dimensions in p2's input order) the
-// coordinate contributes (c >> sh) * mul.  Returns p1's number of tiles.
+// Complex lines of a fast pass along its tile dimension (two real lines per
+// complex line for r2c / c2r).
+static int64_t complex_lines(const Pass& ps) {
+  const int t = tile_dim(ps);
+  const int64_t nt = t >= 0 ? ps.lin.size[t] : 1;
+  return ps.op == OP_C2C ? nt : (nt + 1) / 2;
+}
+
+// Element -> first-pass line map of the second pass of a Float64 run: the
+// first pass p1 numbers its complex lines (coordinate along its tile
+// dimension t1, halved when packed) + ncl1 * (outer index in p1's input
+// order); for each role of p2 (axis, tile dimension, outer dimensions in
+// p2's input order) the coordinate contributes (c >> sh) * mul.  Returns the
+// number of p1's complex lines.
 static int64_t te_mapping(const Pass& p1, Pass& p2) {
   const int a1 = p1.axis, t1 = tile_dim(p1);
-  int sh1 = 0;
-  while ((1 << sh1) < p1.lines) ++sh1;
-  const int64_t ntiles1 = t1 >= 0 ? (p1.lin.size[t1] + p1.lines - 1) / p1.lines : 1;
+  const int sh1 = p1.op == OP_C2C ? 0 : 1;
+  const int64_t ncl1 = complex_lines(p1);
   int64_t mul1[kMaxD] = {};
-  int64_t m = ntiles1;
+  int64_t m = ncl1;
   for (int q = 0; q < p1.lin.D; ++q) {
     const int d = p1.lin.perm[q];
     if (d == a1 || d == t1) continue;
@@ -702,6 +710,7 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.self_scale = ps.self_scale ? 1 : 0;
   F.te_rescale = ps.te_rescale ? 1 : 0;
   F.te = (ps.self_scale && ps.out_dd) || ps.te_rescale ? P->te_dev : nullptr;
+  F.te_ncl = complex_lines(ps);
   for (int i = 0; i < 2 + kMaxOuter; ++i) {
     F.te_sh[i] = ps.te_sh[i];
     F.te_mul[i] = ps.te_mul[i];
