@@ -133,6 +133,25 @@ def test_dd_wide_dynamic_range(cuda):
         assert rel(plan.ldiv(B).to_logical(), x) <= 1e-13
 
 
+@pytest.mark.parametrize("dims, tr", [((64, 32, 16), T.RFFT()), ((16, 8, 4, 6), T.FFT()),
+                                      ((8, 64), (T.FFT(), T.FFT()))])
+def test_dd_line_scales(cuda, dims, tr):
+    """Float64 runs scale each first-pass line by its own largest exponent
+    and rescale in the next pass: lines whose magnitudes differ by up to
+    1e+-60 within one array, and all-zero lines, keep the 1e-13 bound
+    (forward against the oracle and round trip), in both directions."""
+    plan = P.PencilFFTPlan(dims, tr, F64)
+    orc = oracle_plan(plan)
+    rng = np.random.default_rng(11)
+    x = random_input(plan, 11)
+    line_scale = 10.0 ** rng.uniform(-60, 60, size=(1,) + tuple(dims[1:]))
+    line_scale[..., 0] = 0.0  # some lines all zero
+    x = x * line_scale
+    B = plan * input_array(plan, x)
+    assert rel(B.to_logical(), orc.forward(x)) <= 1e-13
+    assert rel(plan.ldiv(B).to_logical(), x) <= 1e-13
+
+
 @pytest.mark.parametrize("n", [7, 11, 13, 17, 23, 41, 53, 97, 191, 384, 1000, 1024, 2048])
 @pytest.mark.parametrize("real", [F64, F32])
 def test_1d_lengths(cuda, n, real):
