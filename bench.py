@@ -355,18 +355,24 @@ def run_gpu(args, rank, world, local_rank):
             e2e_step(k)
         torch.cuda.synchronize()
         barrier()
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(s_in)
-        for k in range(args.steps):
-            e2e_step(k)
-        s_in.wait_stream(s_out)
-        f1.record(s_in)
-        torch.cuda.synchronize()
-        e2e_ms = max_over_ranks(f0.elapsed_time(f1) / args.steps, world, dev)
+        # three timed repetitions of the K steps, median reported: the host
+        # link is shared with other jobs on the machine and varies run to run
+        samples = []
+        for _ in range(3):
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(s_in)
+            for k in range(args.steps):
+                e2e_step(k)
+            s_in.wait_stream(s_out)
+            f1.record(s_in)
+            torch.cuda.synchronize()
+            samples.append(f0.elapsed_time(f1) / args.steps)
+        e2e_ms = max_over_ranks(statistics.median(samples), world, dev)
         nb = host_in.numel() * host_in.element_size()
         e2e = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
-               "pipelined": "copy-in / transforms / copy-out on three streams, double-buffered"}
+               "pipelined": "copy-in / transforms / copy-out on three streams, double-buffered",
+               "samples_ms": samples, "statistic": "median of 3 timed repetitions of the K steps"}
         # the result of the last step round-trips the input
         err = (host_out[(args.steps - 1) & 1].double() - host_in.double()).norm() / host_in.double().norm()
         e2e["round_trip_rel_l2"] = float(err)
