@@ -76,7 +76,11 @@ typedef struct pfgb_plan_desc {
   int32_t n_extra;                    /* number of extra_dims */
   int64_t extra_dims[PFGB_MAX_EXTRA];
   int32_t precision_mode;             /* PFGB_PRECISION_* */
-  int32_t autotune;                   /* 0 = off */
+  int32_t autotune;                   /* 0 = off; 1 = measure at plan creation: time
+                                         the alternative kernels of each pass on
+                                         temporary buffers and keep the faster
+                                         (the reference's fftw_flags = FFTW.MEASURE,
+                                         src/plans.jl:241-320) */
 } pfgb_plan_desc;
 
 /* Arithmetic of the transform kernels.

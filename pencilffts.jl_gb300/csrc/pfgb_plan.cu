@@ -117,6 +117,9 @@ struct Pass {
   unsigned te_mul[2 + kMaxOuter] = {};
   int logm = 0;
   const void* ftw = nullptr;  // its twiddle table (float or dd entries)
+  // kernel variant chosen by the planner's measurement (autotune): -1
+  // default, 0 plain fast_pass, 1 TMA-fed persistent form (c2r passes)
+  int variant = -1;
   // tensor-core split form (Float32 c2c, precision PFGB_PRECISION_TC_SPLIT)
   bool tc = false;
   const void* tcb = nullptr;  // DFT matrices, tf32 hi / lo in operand layout
@@ -792,7 +795,8 @@ int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
 // the plain kernel overlaps load and compute better (Float64 512^3 c2r pass
 // 1.05 ms against 1.09 ms; the TMA form's two tile buffers allow two CTAs).
 static bool tma_eligible(const pfgb_plan* P, const Pass& ps, const FastArgs& F) {
-  if (!PFGB_FAST_TMA || !ps.fast || F.op != OP_C2R || F.lmap_tile || F.in_sa != 1) return false;
+  const bool wanted = ps.variant == 1 || (ps.variant < 0 && PFGB_FAST_TMA);
+  if (!wanted || !ps.fast || F.op != OP_C2R || F.lmap_tile || F.in_sa != 1) return false;
   const int esz = F.op == OP_R2C ? P->rb : 2 * P->rb;
   const int64_t line = (int64_t)(F.op == OP_C2R ? F.n_in : (1 << ps.logm)) * esz;
   if (line % 16) return false;
@@ -1125,6 +1129,8 @@ int pfgb_last_error(char* buf, size_t n) {
   return (int)e.size();
 }
 
+static int autotune_passes(pfgb_plan* P);
+
 static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_only) {
   g_last_error.clear();
   if (!desc || !out) return fail(PFGB_ERR_ARGUMENT, "null argument");
@@ -1306,6 +1312,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
       }
     }
   }
+  if (!rc && !query_only && d.autotune) rc = autotune_passes(P);
   if (rc) {
     pfgb_plan_destroy(P);
     return rc;
@@ -1343,6 +1350,66 @@ int pfgb_plan_set_timing(pfgb_plan* P, int on) {
   return PFGB_OK;
 }
 
+// Planner measurement (desc.autotune; the reference's FFTW.MEASURE planning
+// flag): every pass with alternative kernels runs each of them on temporary
+// buffers filled with normal numbers (bytes 0x3F), and the faster is kept.
+// Alternatives today: c2r passes, plain fast_pass or the TMA-fed persistent
+// form (when the buffers satisfy its alignment).
+static int autotune_passes(pfgb_plan* P) {
+  const int e1023 = 1023;
+  for (auto* dir : {&P->fwd, &P->bwd}) {
+    for (auto& ps : dir->passes) {
+      if (!ps.fast || ps.op != OP_C2R || ps.tc) continue;
+      void* bin = nullptr;
+      void* bout = nullptr;
+      const size_t nin = (size_t)ps.lin.bytes(), nout = (size_t)ps.lout.bytes();
+      PFGB_CUDA(cudaMalloc(&bin, nin));
+      cudaError_t e = cudaMalloc(&bout, nout);
+      if (e != cudaSuccess) {
+        cudaFree(bin);
+        return fail(PFGB_ERR_ALLOC, std::string("cudaMalloc (autotune): ") + cudaGetErrorString(e));
+      }
+      cudaEvent_t ea = nullptr, eb = nullptr;
+      int rc = PFGB_OK;
+      float best[2] = {3.0e38f, 3.0e38f};
+      if ((e = cudaMemset(bin, 0x3F, nin)) != cudaSuccess ||
+          (e = cudaMemcpy(P->emax_dev, &e1023, sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+          (e = cudaEventCreate(&ea)) != cudaSuccess || (e = cudaEventCreate(&eb)) != cudaSuccess)
+        rc = fail_cuda(e, "autotune set-up");
+      for (int v = 0; v < 2 && !rc; ++v) {
+        ps.variant = v;
+        FastArgs F;
+        int64_t grid = 0;
+        rc = make_fast_args(P, ps, bin, bout, false, F, grid);
+        if (rc || (v == 1 && !tma_eligible(P, ps, F))) break;
+        for (int it = 0; it < 7 && !rc; ++it) {
+          cudaEventRecord(ea, 0);
+          if (v == 0) {
+            rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, 0) : launch_fast_f32(ps.logm, ps.sign, F, grid, 0);
+          } else {
+            F.total = grid;
+            F.err = P->emax_dev + 1;
+            rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, 0) : launch_fast_tma_f32(ps.logm, ps.sign, F, 0);
+          }
+          cudaEventRecord(eb, 0);
+          if ((e = cudaEventSynchronize(eb)) != cudaSuccess) rc = fail_cuda(e, "autotune launch");
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, ea, eb);
+          if (it >= 2 && ms < best[v]) best[v] = ms;
+        }
+      }
+      ps.variant = best[1] < best[0] ? 1 : 0;
+      if (ea) cudaEventDestroy(ea);
+      if (eb) cudaEventDestroy(eb);
+      cudaFree(bin);
+      cudaFree(bout);
+      if (rc) return rc;
+    }
+  }
+  PFGB_CUDA(cudaMemset(P->emax_dev, 0, 16));  // exponent and error words
+  return PFGB_OK;
+}
+
 int pfgb_device_status(pfgb_plan* P, void* stream, int32_t* flags) {
   if (!P || !flags) return fail(PFGB_ERR_ARGUMENT, "null argument");
   *flags = 0;
@@ -1374,6 +1441,7 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     e.bytes_per_launch = red ? ps.lin.bytes() : ps.lin.bytes() + ps.lout.bytes();
     const char* kname = red ? "emax_kernel" : ps.pk == PK_COPY ? "copy_kernel"
                         : ps.tc ? "tc_pass<tf32x3>"
+                        : ps.variant == 1 ? (P->rb == 8 ? "fast_pass_tma<dd>" : "fast_pass_tma<float>")
                         : ps.fast ? (P->rb == 8 ? "fast_pass<dd>" : "fast_pass<float>")
                                   : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);

@@ -6,7 +6,8 @@ The API mirrors the reference's ``PencilFFTPlan`` / ``Transforms`` interface at
 """
 from . import transforms as Transforms
 from ._lib import ArgumentError, LibraryError, load as load_library
-from .plans import (Batch, ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
+from .plans import (FFTW_ESTIMATE, FFTW_EXHAUSTIVE, FFTW_MEASURE, FFTW_PATIENT, Batch,
+                    ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
                     allocate_input, allocate_output, bmul_, gather, is_inplace,
                     ldiv, ldiv_, mul_, plan_query, scale_factor)
 
@@ -14,4 +15,5 @@ __all__ = [
     "Transforms", "Batch", "ArgumentError", "LibraryError", "load_library", "ManyPencilArray",
     "Pencil", "PencilArray", "PencilFFTPlan", "Val", "allocate_input", "allocate_output",
     "bmul_", "gather", "is_inplace", "ldiv", "ldiv_", "mul_", "plan_query", "scale_factor",
+    "FFTW_ESTIMATE", "FFTW_MEASURE", "FFTW_PATIENT", "FFTW_EXHAUSTIVE",
 ]

@@ -182,8 +182,24 @@ def _expand(transforms, N):
 
 PRECISION = {"default": 0, "native": 1, "tc": 2}
 
+# FFTW planner flags (FFTW.jl values); PencilFFTs passes fftw_flags to FFTW's
+# planner, default FFTW.ESTIMATE (reference src/plans.jl:241-320)
+FFTW_MEASURE, FFTW_EXHAUSTIVE, FFTW_PATIENT, FFTW_ESTIMATE = 0, 1 << 3, 1 << 5, 1 << 6
 
-def _descriptor(dims, transforms, real_type, permute_dims, extra_dims, precision="default") -> PlanDesc:
+
+def _autotune_from(fftw_flags, autotune):
+    """Planner measurement on (1) when requested explicitly, or when the FFTW
+    planner flags ask for anything beyond FFTW.ESTIMATE, as FFTW would
+    measure its candidate plans."""
+    if autotune is not None:
+        return 1 if autotune else 0
+    if fftw_flags is None:
+        return 0
+    return 0 if int(fftw_flags) & FFTW_ESTIMATE else 1
+
+
+def _descriptor(dims, transforms, real_type, permute_dims, extra_dims, precision="default",
+                autotune=0) -> PlanDesc:
     N = len(dims)
     if N < 1 or N > _lib.MAX_DIMS:
         raise ArgumentError(f"number of dimensions must be in [1, {_lib.MAX_DIMS}]")
@@ -208,7 +224,7 @@ def _descriptor(dims, transforms, real_type, permute_dims, extra_dims, precision
     if precision not in PRECISION:
         raise ArgumentError(f"precision must be one of {tuple(PRECISION)}")
     d.precision_mode = PRECISION[precision]
-    d.autotune = 0
+    d.autotune = int(autotune)
     return d
 
 
@@ -234,15 +250,17 @@ class PencilFFTPlan:
     pipes for power-of-two lines, FP64 elsewhere), "native" (Float64 plans:
     FP64 everywhere) or "tc" (Float32 plans: c2c lines of 256, 512 and 1024
     points as tensor-core DFT-matrix products with a tf32 hi/lo split; rel. L2
-    about 1e-6).  FFTW planning keywords
-    (``fftw_flags``, ``fftw_timelimit``) and ``transpose_method`` are accepted
-    and ignored, as the reference does for GPU arrays (src/plans.jl:325-332).
+    about 1e-6).  ``fftw_flags`` other than FFTW.ESTIMATE (e.g. FFTW.MEASURE =
+    0), or ``autotune=True``, make plan creation time the alternative kernels
+    of each pass and keep the faster, as FFTW measures its candidates.
+    ``fftw_timelimit`` and ``transpose_method`` are accepted and ignored, as
+    the reference does for GPU arrays (src/plans.jl:325-332).
     """
 
     def __init__(self, dims_global, transforms, real_type=np.float64, *,
                  proc_dims=None, permute_dims=True, extra_dims=(),
                  fftw_flags=None, fftw_timelimit=None, transpose_method=None,
-                 timer=None, stream=None, precision="default"):
+                 timer=None, stream=None, precision="default", autotune=None):
         dims = tuple(int(x) for x in dims_global)
         if proc_dims is not None and any(int(p) != 1 for p in proc_dims):
             raise ArgumentError("this implementation runs on one GPU: proc_dims must be all ones")
@@ -258,8 +276,9 @@ class PencilFFTPlan:
         self.timer = timer
         self._stream = stream
         self.precision = precision
+        self.autotune = _autotune_from(fftw_flags, autotune)
         desc = _descriptor(dims, self.transforms, self.real_type, self.permute_dims, self.extra_dims,
-                           precision)
+                           precision, self.autotune)
         L = _lib.load()
         handle = ctypes.c_void_p()
         _lib.check(L.pfgb_plan_create(ctypes.byref(desc), ctypes.byref(handle)), "pfgb_plan_create")

@@ -176,3 +176,16 @@ def test_tc_split_precision_descriptor():
         P.plan_query((64, 512, 256), T.FFT(), np.float64, precision="tc")
     with pytest.raises(P.ArgumentError, match="precision"):
         P.plan_query((8, 8), T.FFT(), np.float32, precision="bf16")
+
+
+def test_fftw_flags_select_measurement():
+    """FFTW.ESTIMATE (the reference's default) plans without measuring; any
+    other planner flag, or autotune=True, measures."""
+    from pencilffts_gb300.plans import _autotune_from
+    assert _autotune_from(None, None) == 0
+    assert _autotune_from(P.FFTW_ESTIMATE, None) == 0
+    assert _autotune_from(P.FFTW_MEASURE, None) == 1
+    assert _autotune_from(P.FFTW_PATIENT, None) == 1
+    assert _autotune_from(P.FFTW_ESTIMATE, True) == 1
+    assert _autotune_from(P.FFTW_MEASURE, False) == 0
+    P.plan_query((64, 48, 32), T.RFFT())  # host-only analysis never measures

@@ -139,3 +139,21 @@ def test_batch_graph_replay(cuda):
         for p, v, w, x in zip(plans, vs, ws, xs):
             assert rel(v.to_logical(), oracle_plan(p).forward(x)) <= 2e-6
             assert rel(w.to_logical(), x) <= 2e-6
+
+
+@pytest.mark.parametrize("real", [np.float64, np.float32])
+def test_autotune_measure(cuda, real):
+    """fftw_flags = FFTW.MEASURE (or autotune=True) times the alternative
+    kernels of each pass at plan creation; the results are those of the
+    default plan (both kernels run the same arithmetic)."""
+    dims = (64, 48, 32)
+    plan = P.PencilFFTPlan(dims, T.RFFT(), real, fftw_flags=P.FFTW_MEASURE)
+    assert plan.autotune == 1
+    assert P.PencilFFTPlan(dims, T.RFFT(), real, fftw_flags=P.FFTW_ESTIMATE).autotune == 0
+    ref = P.PencilFFTPlan(dims, T.RFFT(), real)
+    x = np.random.default_rng(3).standard_normal(dims).astype(real)
+    v, vref = plan * input_array(plan, x), ref * input_array(ref, x)
+    assert np.array_equal(v.to_logical(), vref.to_logical())
+    w, wref = plan.ldiv(v), ref.ldiv(vref)
+    assert np.array_equal(w.to_logical(), wref.to_logical())
+    assert plan.device_status() == 0
