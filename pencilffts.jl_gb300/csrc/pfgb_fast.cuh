@@ -395,13 +395,17 @@ __device__ __forceinline__ int line_exponent(unsigned emx, const FastArgs& a, un
 __device__ __forceinline__ unsigned dexp_u(double x) {
   return (unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu;
 }
-// 2^(te[tile1] - run exponent) for the element at axis coordinate pos of the
-// line at coordinate line along the tile dimension (te_rescale)
-__device__ __forceinline__ float te_factor(const FastArgs& a, unsigned tebase, int64_t line, int pos, int erun) {
-  const unsigned t1 = tebase + ((unsigned)line >> a.te_sh[1]) * a.te_mul[1] +
-                      ((unsigned)pos >> a.te_sh[0]) * a.te_mul[0];
-  const int d = __ldg(a.te + t1) - erun;
+// First-pass line of the element at axis coordinate pos of the line at
+// coordinate line along the tile dimension (te_rescale), its recorded
+// exponent, and 2^(d) for the difference d to the run exponent (d <= 0).
+__device__ __forceinline__ unsigned te_index(const FastArgs& a, unsigned tebase, int64_t line, int pos) {
+  return tebase + ((unsigned)line >> a.te_sh[1]) * a.te_mul[1] + ((unsigned)pos >> a.te_sh[0]) * a.te_mul[0];
+}
+__device__ __forceinline__ float pow2_le0(int d) {
   return d >= -126 ? __uint_as_float((unsigned)(d + 127) << 23) : 0.0f;
+}
+__device__ __forceinline__ float te_factor(const FastArgs& a, unsigned tebase, int64_t line, int pos, int erun) {
+  return pow2_le0(__ldg(a.te + te_index(a, tebase, line, pos)) - erun);
 }
 template <typename R>
 __device__ __forceinline__ Cx<R> scale_pow2(Cx<R> y, float f) {
@@ -448,14 +452,25 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   if (a.op == OP_C2C) {
     if (IO::kDD && a.in_dd) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
+      // exponents of the elements' first-pass lines, loaded ahead of the data
+      int tev[8];
+      if (IO::kDD && a.te_rescale) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) tev[r] = p < nvalid ? __ldg(a.te + te_index(a, o.tebase, t0 + p, b + r * T)) : emax;
+      }
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
         const float4 q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : make_float4(0.f, 0.f, 0.f, 0.f);
         v[r] = ld_dd4<R>(q);
       }
-      if (IO::kDD && a.te_rescale && p < nvalid) {
+      if (IO::kDD && a.te_rescale) {
+        bool off = false;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = scale_pow2(v[r], te_factor(a, o.tebase, t0 + p, b + r * T, emax));
+        for (int r = 0; r < 8; ++r) off |= tev[r] != emax;
+        if (__any_sync(0xFFFFFFFFu, off)) {  // lines below the run exponent in this warp
+#pragma unroll
+          for (int r = 0; r < 8; ++r) v[r] = scale_pow2(v[r], pow2_le0(tev[r] - emax));
+        }
       }
     } else {
       // all loads first, conversions after: the conversion's rare-case
