@@ -94,11 +94,11 @@ __device__ __forceinline__ Cx<R> mul_ik(Cx<R> y, int64_t idx, int half, int64_t 
 
 // Threads per CTA of the fast pass (8 points of one line per thread) and
 // CTAs per SM, measured on GB300 (512^3 round trip):
-//   dd:    256 threads, 3 CTAs/SM (80 registers): the CTAs' load and
+//   dd:    256 threads, 4 CTAs/SM (64 registers): the CTAs' load and
 //          compute phases interleave (two CTAs: 5.87 ms against 6.58 ms with
-//          one 512-thread CTA; three: 5.43 ms against 5.63 ms with two;
-//          128-thread CTAs: 5.81 ms); 512 threads when a line needs them
-//          (M = 4096).
+//          one 512-thread CTA; three: 5.43 ms against 5.63 ms with two; four:
+//          4.70 ms against 4.91 ms with three; 128-thread CTAs: 5.81 ms);
+//          512 threads when a line needs them (M = 4096).
 //   float: 512 threads, 3 CTAs/SM (register cap 42): 1.75 ms against 1.84 ms
 //          with 2 CTAs/SM and 1.80 ms with four 256-thread CTAs.
 #ifndef PFGB_FAST_THREADS_F32
@@ -303,11 +303,13 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 #ifndef PFGB_FAST_F32_MINBLOCKS
 #define PFGB_FAST_F32_MINBLOCKS 3
 #endif
-// dd CTAs of 256 threads: three per SM (80 registers, <= 8 bytes of spill)
-// measured 5.43 ms against 5.63 ms with two (123 registers) per 512^3 round
-// trip; 0 selects 128 registers a thread (512 / threads CTAs).
+// dd CTAs of 256 threads: four per SM (64 registers, 64-140 bytes of spill
+// a thread), measured per 512^3 round trip: 4.70 ms against 4.91 ms with
+// three (80 registers) and, in an earlier build, 5.43 against 5.63 ms for
+// three against two (123 registers): this issue-bound kernel gains more from
+// resident warps than it loses to spills.  0 selects 128 registers a thread.
 #ifndef PFGB_FAST_DD_MINBLOCKS
-#define PFGB_FAST_DD_MINBLOCKS 3
+#define PFGB_FAST_DD_MINBLOCKS 4
 #endif
 template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm) {
