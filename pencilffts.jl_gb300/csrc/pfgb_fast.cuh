@@ -419,7 +419,7 @@ __device__ __forceinline__ Cx<R> scale_pow2(Cx<R> y, float f) {
 // a copy of the tile's input lines in shared memory), stages, store.  `src`
 // is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
 // offset in the pass input).
-template <typename R, int LOGM, int SIGN>
+template <typename R, int LOGM, int SIGN, int OP>
 __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
                                           int64_t soff, int64_t ssa, int64_t sst) {
   using IO = FastIO<R>;
@@ -433,7 +433,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   int p, b;
   if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
 
-  const bool packed = a.op != OP_C2C;
+  const bool packed = OP != OP_C2C;
   const int lines = packed ? 2 * TW : TW;
   const TileOrigin o = tile_origin(a, (unsigned)bid, lines);
   const int64_t t0 = o.t0, ooff = o.ooff, didx = o.didx;
@@ -451,7 +451,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       emax_out = emax + a.emax_shift;
     }
   }
-  if (a.op == OP_C2C) {
+  if constexpr (OP == OP_C2C) {
     if (IO::kDD && a.in_dd) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
       // exponents of the elements' first-pass lines, loaded ahead of the data
@@ -500,7 +500,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
       }
     }
-  } else if (a.op == OP_R2C) {
+  } else if constexpr (OP == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
     MR ra[8], rb[8];
@@ -580,15 +580,15 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   fast_stages<R, LOGM, SIGN>(v, z, p, b, a.tw, a.lmap_tile != 0);
 
   // ---- store ----
-  if (a.deriv == 2 && a.store_direct && a.op == OP_C2C) {
+  if (a.deriv == 2 && a.store_direct && OP == OP_C2C) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
       v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
     }
   }
-  if (a.store_direct && a.op != OP_R2C) {
-    if (a.op == OP_C2C) {
+  if (a.store_direct && OP != OP_R2C) {
+    if constexpr (OP == OP_C2C) {
       if (p < nvalid) {
         if (IO::kDD && a.out_dd) {
           float4* out = reinterpret_cast<float4*>(a.out) + ooff + (int64_t)p * a.out_st;
@@ -631,7 +631,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   // output exponent of complex line i (the first pass of a run scales lines
   // separately; the loops below write other threads' lines)
   auto line_emax_out = [&](int i) { return IO::kDD && a.self_scale ? lexp[i] + a.emax_shift : emax_out; };
-  if (a.op == OP_C2C) {
+  if constexpr (OP == OP_C2C) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
     const int tot = TW * M;
     for (int e = tid; e < tot; e += nth) {
@@ -653,7 +653,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = o;
       }
     }
-  } else if (a.op == OP_R2C) {
+  } else if constexpr (OP == OP_R2C) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
     const int m = a.n_out;
     const int tot = TW * m;
@@ -703,10 +703,13 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   }
 }
 
-template <typename R, int LOGM, int SIGN>
+// One kernel per operation (c2c, r2c, c2r): each keeps only its own load and
+// store paths, which frees registers (c2c at 64 registers: 8-16 bytes of
+// spill against 96-140 bytes with all three paths in one kernel).
+template <typename R, int LOGM, int SIGN, int OP>
 __global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM)) fast_pass(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  fast_tile<R, LOGM, SIGN>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
+  fast_tile<R, LOGM, SIGN, OP>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
 }
 
 // ---------------------------------------------------------------------------
@@ -826,7 +829,7 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), tma_min_blocks<R>(LOGM)
     if (!mbar_wait_bounded(&bars[it & 1], (it >> 1) & 1)) s_fail = 1;
     __syncthreads();
     if (s_fail) break;
-    fast_tile<R, LOGM, SIGN>(a, tile, z, buf0 + (it & 1) * tb, 0, 1, line_elems);
+    fast_tile<R, LOGM, SIGN, OP_C2R>(a, tile, z, buf0 + (it & 1) * tb, 0, 1, line_elems);
     __syncthreads();
   }
   if (s_fail && threadIdx.x == 0) {

@@ -1,0 +1,15 @@
+// Register Stockham pass, double-float (dd) arithmetic for Float64 data, c2r lines.
+#include "pfgb_fast_launch.cuh"
+
+namespace pfgb {
+
+int launch_fast_dd_c2r(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op<dd, OP_C2R>(logm, sign, A, grid, s);
+}
+
+// TMA-fed persistent form (c2r passes); A.total == 0 only configures it.
+int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s) {
+  return sign < 0 ? launch_tma_sign<dd, -1>(logm, A, s) : launch_tma_sign<dd, 1>(logm, A, s);
+}
+
+}  // namespace pfgb

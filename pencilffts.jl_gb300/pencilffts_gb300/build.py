@@ -22,7 +22,8 @@ LIB = os.path.join(LIBDIR, "libpencilfft_gb300.so")
 INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["pfgb_plan.cu", "pfgb_kernels.cu", "pfgb_fast_f32.cu", "pfgb_fast_dd.cu", "pfgb_noalloc.cu", "pfgb_tc.cu"]
+SOURCES = ["pfgb_plan.cu", "pfgb_kernels.cu", "pfgb_noalloc.cu", "pfgb_tc.cu"] + [
+    f"pfgb_fast_{t}_{op}.cu" for t in ("f32", "dd") for op in ("c2c", "r2c", "c2r")]
 
 
 def _nvcc():
