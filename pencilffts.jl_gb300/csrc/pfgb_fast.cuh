@@ -303,20 +303,27 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 #ifndef PFGB_FAST_F32_MINBLOCKS
 #define PFGB_FAST_F32_MINBLOCKS 3
 #endif
-// dd CTAs of 256 threads: four per SM (64 registers, 64-140 bytes of spill
-// a thread), measured per 512^3 round trip: 4.70 ms against 4.91 ms with
-// three (80 registers) and, in an earlier build, 5.43 against 5.63 ms for
-// three against two (123 registers): this issue-bound kernel gains more from
-// resident warps than it loses to spills.  0 selects 128 registers a thread.
+// dd CTAs of 256 threads: four per SM (64 registers), measured per 512^3
+// round trip: 4.52 ms against 4.63 ms with five (48 registers, 20-56 bytes of
+// spill) and 4.91 ms with three (80 registers); in an earlier build three
+// against two (123 registers) gave 5.43 against 5.63 ms: this issue-bound
+// kernel gains from resident warps until spills take over.  The variants
+// (operation, dd or double input, dd or double output) are separate kernels
+// so that each allocates registers for its own paths only (at 64 registers
+// 0-16 bytes of spill, against 96-140 with all paths in one kernel).  A c2r
+// pass with double input would spill 0.4-0.6 KB at 48 registers and stays at
+// four when more are asked for.  0 selects 128 registers a thread.
 #ifndef PFGB_FAST_DD_MINBLOCKS
 #define PFGB_FAST_DD_MINBLOCKS 4
 #endif
+// kernel variant: operation OP and IOM = dd input (bit 0) | dd output (bit 1)
 template <typename R>
-__host__ __device__ constexpr int fast_min_blocks(int logm) {
+__host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
   return sizeof(R) == 4 ? PFGB_FAST_F32_MINBLOCKS
          : fast_threads<R>(logm) >= 512 ? 1
-         : PFGB_FAST_DD_MINBLOCKS > 0 ? PFGB_FAST_DD_MINBLOCKS
-                                      : 512 / fast_threads<R>(logm);
+         : PFGB_FAST_DD_MINBLOCKS <= 0 ? 512 / fast_threads<R>(logm)
+         : (op == OP_C2R && !(iom & 1) && PFGB_FAST_DD_MINBLOCKS > 4) ? 4
+                                                                     : PFGB_FAST_DD_MINBLOCKS;
 }
 
 // Origin of tile `bid` (< 2^31) of a pass: first line t0 along the tile
@@ -419,10 +426,12 @@ __device__ __forceinline__ Cx<R> scale_pow2(Cx<R> y, float f) {
 // a copy of the tile's input lines in shared memory), stages, store.  `src`
 // is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
 // offset in the pass input).
-template <typename R, int LOGM, int SIGN, int OP>
+template <typename R, int LOGM, int SIGN, int OP, int IOM>
 __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
                                           int64_t soff, int64_t ssa, int64_t sst) {
   using IO = FastIO<R>;
+  constexpr bool IN_DD = IO::kDD && (IOM & 1) != 0;   // input in dd form
+  constexpr bool OUT_DD = IO::kDD && (IOM & 2) != 0;  // output in dd form
   using MR = typename IO::MR;
   using MC = typename IO::MC;
   constexpr int M = 1 << LOGM;
@@ -452,7 +461,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
     }
   }
   if constexpr (OP == OP_C2C) {
-    if (IO::kDD && a.in_dd) {
+    if (IO::kDD && IN_DD) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
       // exponents of the elements' first-pass lines, loaded ahead of the data
       int tev[8];
@@ -525,7 +534,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
     const int m = a.n_in;
     const int i0 = 2 * p, i1 = 2 * p + 1;
     MC ra[8], rb[8];
-    if (!(IO::kDD && a.in_dd)) {
+    if (!(IO::kDD && IN_DD)) {
       const MC* in = reinterpret_cast<const MC*>(src) + ioff;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
@@ -551,7 +560,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       const int k = pos < m ? pos : M - pos;
       const int64_t off = (int64_t)k * ssa;
       Cx<R> A, B;
-      if (IO::kDD && a.in_dd) {
+      if (IO::kDD && IN_DD) {
         const float4* in = reinterpret_cast<const float4*>(src) + ioff;
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         A = ld_dd4<R>(i0 < nvalid ? in[off + (int64_t)i0 * sst] : z4);
@@ -590,7 +599,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   if (a.store_direct && OP != OP_R2C) {
     if constexpr (OP == OP_C2C) {
       if (p < nvalid) {
-        if (IO::kDD && a.out_dd) {
+        if (IO::kDD && OUT_DD) {
           float4* out = reinterpret_cast<float4*>(a.out) + ooff + (int64_t)p * a.out_st;
 #pragma unroll
           for (int r = 0; r < 8; ++r) out[(int64_t)(b + r * T) * a.out_sa] = st_dd4(apply_scale(v[r], a));
@@ -643,7 +652,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         const int64_t idx = a.deriv_role == 0 ? (int64_t)k : a.deriv_role == 1 ? t0 + i : didx;
         y = mul_ik(y, idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
       }
-      if (IO::kDD && a.out_dd) {
+      if (IO::kDD && OUT_DD) {
         reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
       } else {
         const int eo = line_emax_out(i);
@@ -667,7 +676,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       B = apply_scale(mk(half(B.re), half(B.im)), a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
-      if (IO::kDD && a.out_dd) {
+      if (IO::kDD && OUT_DD) {
         float4* o4 = reinterpret_cast<float4*>(out);
         if (i0 < nvalid) o4[off + (int64_t)i0 * a.out_st] = st_dd4(A);
         if (i1 < nvalid) o4[off + (int64_t)i1 * a.out_st] = st_dd4(B);
@@ -703,13 +712,15 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   }
 }
 
-// One kernel per operation (c2c, r2c, c2r): each keeps only its own load and
-// store paths, which frees registers (c2c at 64 registers: 8-16 bytes of
-// spill against 96-140 bytes with all three paths in one kernel).
-template <typename R, int LOGM, int SIGN, int OP>
-__global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM)) fast_pass(const FastArgs a) {
+// One kernel per variant (operation c2c / r2c / c2r, dd or double input and
+// output): each keeps only its own load and store paths, which frees
+// registers (c2c at 64 registers: 8-16 bytes of spill against 96-140 bytes
+// with all three operations in one kernel).
+template <typename R, int LOGM, int SIGN, int OP, int IOM>
+__global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM, OP, IOM))
+    fast_pass(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  fast_tile<R, LOGM, SIGN, OP>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
+  fast_tile<R, LOGM, SIGN, OP, IOM>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
 }
 
 // ---------------------------------------------------------------------------
@@ -802,7 +813,7 @@ __host__ __device__ constexpr int tma_min_blocks(int logm) {
   return sizeof(R) == 4 ? 2 : (fast_threads<R>(logm) <= 256 ? 2 : 1);
 }
 
-template <typename R, int LOGM, int SIGN>
+template <typename R, int LOGM, int SIGN, int IOM>
 __global__ void __launch_bounds__(fast_threads<R>(LOGM), tma_min_blocks<R>(LOGM)) fast_pass_tma(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bars[2];
@@ -829,7 +840,7 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM), tma_min_blocks<R>(LOGM)
     if (!mbar_wait_bounded(&bars[it & 1], (it >> 1) & 1)) s_fail = 1;
     __syncthreads();
     if (s_fail) break;
-    fast_tile<R, LOGM, SIGN, OP_C2R>(a, tile, z, buf0 + (it & 1) * tb, 0, 1, line_elems);
+    fast_tile<R, LOGM, SIGN, OP_C2R, IOM>(a, tile, z, buf0 + (it & 1) * tb, 0, 1, line_elems);
     __syncthreads();
   }
   if (s_fail && threadIdx.x == 0) {

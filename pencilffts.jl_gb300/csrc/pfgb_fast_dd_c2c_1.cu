@@ -1,0 +1,10 @@
+// Register Stockham pass, double-float (dd) arithmetic for Float64 data, c2c lines, dd input, double output.
+#include "pfgb_fast_launch.cuh"
+
+namespace pfgb {
+
+int launch_fast_dd_c2c_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op<dd, OP_C2C, 1>(logm, sign, A, grid, s);
+}
+
+}  // namespace pfgb

@@ -1,0 +1,14 @@
+// Register Stockham pass, double-float (dd) arithmetic for Float64 data, c2r lines, dd input, double output.
+#include "pfgb_fast_launch.cuh"
+
+namespace pfgb {
+
+int launch_fast_dd_c2r_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op<dd, OP_C2R, 1>(logm, sign, A, grid, s);
+}
+
+int launch_fast_tma_dd_1(int logm, int sign, const FastArgs& A, cudaStream_t s) {
+  return sign < 0 ? launch_tma_sign<dd, -1, 1>(logm, A, s) : launch_tma_sign<dd, 1, 1>(logm, A, s);
+}
+
+}  // namespace pfgb

@@ -3,19 +3,21 @@
 
 namespace pfgb {
 
-int launch_fast_f32_r2c(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
-int launch_fast_f32_c2r(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_f32_r2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_f32_c2r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
-int launch_fast_f32_c2c(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
-  return launch_fast_op<float, OP_C2C>(logm, sign, A, grid, s);
+int launch_fast_f32_c2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op<float, OP_C2C, 0>(logm, sign, A, grid, s);
 }
 
-// Entry point of the pass kernels of this type: dispatch on the operation.
+// Entry point of the pass kernels of this type: dispatch on the operation
+// and on the input / output form.
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
-  switch (A.op) {
-    case OP_C2C: return launch_fast_f32_c2c(logm, sign, A, grid, s);
-    case OP_R2C: return launch_fast_f32_r2c(logm, sign, A, grid, s);
-    case OP_C2R: return launch_fast_f32_c2r(logm, sign, A, grid, s);
+  const int iom = 0;
+  switch (A.op * 4 + iom) {
+    case OP_C2C * 4 + 0: return launch_fast_f32_c2c_0(logm, sign, A, grid, s);
+    case OP_R2C * 4 + 0: return launch_fast_f32_r2c_0(logm, sign, A, grid, s);
+    case OP_C2R * 4 + 0: return launch_fast_f32_c2r_0(logm, sign, A, grid, s);
     default: return PFGB_ERR_UNSUPPORTED;
   }
 }

@@ -3,8 +3,8 @@
 
 namespace pfgb {
 
-int launch_fast_f32_r2c(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
-  return launch_fast_op<float, OP_R2C>(logm, sign, A, grid, s);
+int launch_fast_f32_r2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op<float, OP_R2C, 0>(logm, sign, A, grid, s);
 }
 
 }  // namespace pfgb

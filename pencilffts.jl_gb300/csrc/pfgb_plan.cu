@@ -1245,30 +1245,6 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   for (auto* dir : {&P->fwd, &P->bwd})
     for (auto& ps : dir->passes)
       if (!rc) rc = prepare_pass(P, ps);
-  // set the shared-memory opt-in of every kernel the plan launches now, so that
-  // executions recorded into a CUDA graph only launch
-  if (!rc && !query_only) {
-    for (auto* dir : {&P->fwd, &P->bwd}) {
-      for (auto& ps : dir->passes) {
-        if (rc || ps.pk != PK_TRANSFORM) continue;
-        if (ps.fast) {
-          FastArgs F;
-          std::memset(&F, 0, sizeof(F));
-          F.op = ps.op;
-          rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
-                          : launch_fast_f32(ps.logm, ps.sign, F, 0, nullptr);
-          if (!rc && PFGB_FAST_TMA)
-            rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
-                            : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);
-          if (!rc && ps.tc) rc = launch_tc(ps.logm, ps.sign, F, nullptr);
-        } else {
-          PassArgs A;
-          std::memset(&A, 0, sizeof(A));
-          rc = launch_pass(P->rb, A, 0, 0, 0, nullptr);
-        }
-      }
-    }
-  }
   // Float64 runs of consecutive fast passes exchange data in dd form
   int64_t te_tiles = 0;
   if (!rc && P->rb == 8) {
@@ -1288,6 +1264,32 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
           v[i + 1].te_rescale = true;
           te_tiles = std::max(te_tiles, te_mapping(v[i], v[i + 1]));
         }
+    }
+  }
+  // set the shared-memory opt-in of every kernel the plan launches now, so that
+  // executions recorded into a CUDA graph only launch
+  if (!rc && !query_only) {
+    for (auto* dir : {&P->fwd, &P->bwd}) {
+      for (auto& ps : dir->passes) {
+        if (rc || ps.pk != PK_TRANSFORM) continue;
+        if (ps.fast) {
+          FastArgs F;
+          std::memset(&F, 0, sizeof(F));
+          F.op = ps.op;
+          F.in_dd = ps.in_dd ? 1 : 0;  // selects the kernel variant
+          F.out_dd = ps.out_dd ? 1 : 0;
+          rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
+                          : launch_fast_f32(ps.logm, ps.sign, F, 0, nullptr);
+          if (!rc && PFGB_FAST_TMA)
+            rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
+                            : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);
+          if (!rc && ps.tc) rc = launch_tc(ps.logm, ps.sign, F, nullptr);
+        } else {
+          PassArgs A;
+          std::memset(&A, 0, sizeof(A));
+          rc = launch_pass(P->rb, A, 0, 0, 0, nullptr);
+        }
+      }
     }
   }
   if (!rc && !query_only && te_tiles > 0) {
