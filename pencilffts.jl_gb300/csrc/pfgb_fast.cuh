@@ -300,8 +300,10 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
   }
 }
 
+// float CTAs of 512 threads: four per SM (32 registers, no spill) for c2c
+// and r2c kernels, three (40 registers) for c2r, which spills at 32
 #ifndef PFGB_FAST_F32_MINBLOCKS
-#define PFGB_FAST_F32_MINBLOCKS 3
+#define PFGB_FAST_F32_MINBLOCKS 4
 #endif
 // dd CTAs of 256 threads: four per SM (64 registers), measured per 512^3
 // round trip: 4.52 ms against 4.63 ms with five (48 registers, 20-56 bytes of
@@ -319,7 +321,7 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 // kernel variant: operation OP and IOM = dd input (bit 0) | dd output (bit 1)
 template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
-  return sizeof(R) == 4 ? PFGB_FAST_F32_MINBLOCKS
+  return sizeof(R) == 4 ? (op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS)
          : fast_threads<R>(logm) >= 512 ? 1
          : PFGB_FAST_DD_MINBLOCKS <= 0 ? 512 / fast_threads<R>(logm)
          : (op == OP_C2R && !(iom & 1) && PFGB_FAST_DD_MINBLOCKS > 4) ? 4
