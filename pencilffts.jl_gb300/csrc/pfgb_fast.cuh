@@ -12,8 +12,9 @@
 // the tile dimension (axis-strided layouts).
 //
 // R is the arithmetic type: float, or dd (double-float on the FP32 pipes) for
-// Float64 data; dd tiles are scaled by a power of two (the tile's largest
-// exponent) so that any finite double range fits the float exponent range.
+// Float64 data; dd data are scaled by powers of two (each line's largest
+// exponent in the first pass of a run, the run's largest afterwards) so that
+// any finite double range fits the float exponent range.
 #pragma once
 
 #include <type_traits>
@@ -35,9 +36,10 @@ struct FastArgs {
   int scale_on;
   float scale_h, scale_l;  // ldiv! normalisation as hi + lo
   // Float64 (dd) passes: the input / output of a pass between two dd passes is
-  // kept in dd form (re.hi, re.lo, im.hi, im.lo floats), scaled by the run's
-  // power of two 2^(1023 - *emax) where *emax is the largest biased exponent of
-  // the run's double input (computed by emax_kernel before the run).
+  // kept in dd form (re.hi, re.lo, im.hi, im.lo floats), scaled by the power
+  // of two 2^(1023 - *emax), *emax the run exponent (see self_scale below;
+  // callers that set neither self_scale nor te_rescale, the allocation-free
+  // entry point, compute it with emax_kernel before the pass).
   int in_dd, out_dd;
   const int* emax_ptr;
   // added to the run exponent for the double outputs of the pass: the ldiv!

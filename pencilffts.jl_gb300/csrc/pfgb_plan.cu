@@ -1436,12 +1436,11 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     std::memset(&e, 0, sizeof(e));
     e.direction = dir;
     e.pass = pass;
-    const bool red = pass >= 100;
-    const Pass& ps = (dir > 0 ? P->fwd : P->bwd).passes[red ? pass - 100 : pass];
+    const Pass& ps = (dir > 0 ? P->fwd : P->bwd).passes[pass];
     e.axis = ps.axis;
-    e.op = red ? -2 : ps.pk == PK_COPY ? -1 : ps.op;
-    e.bytes_per_launch = red ? ps.lin.bytes() : ps.lin.bytes() + ps.lout.bytes();
-    const char* kname = red ? "emax_kernel" : ps.pk == PK_COPY ? "copy_kernel"
+    e.op = ps.pk == PK_COPY ? -1 : ps.op;
+    e.bytes_per_launch = ps.lin.bytes() + ps.lout.bytes();
+    const char* kname = ps.pk == PK_COPY ? "copy_kernel"
                         : ps.tc ? "tc_pass<tf32x3>"
                         : ps.variant == 1 ? (P->rb == 8 ? "fast_pass_tma<dd>" : "fast_pass_tma<float>")
                         : ps.fast ? (P->rb == 8 ? "fast_pass<dd>" : "fast_pass<float>")
