@@ -33,6 +33,7 @@ struct FastArgs {
   int lmap_tile;     // lanes along the tile dimension (tile dim contiguous in input)
   int store_direct;  // store from registers with the load mapping
   int out_tfast;     // tile dimension contiguous in the output (smem store loop)
+  int vec2;          // float r2c: lines 2j, 2j+1 adjacent and 16-byte aligned in the output
   int scale_on;
   float scale_h, scale_l;  // ldiv! normalisation as hi + lo
   // Float64 (dd) passes: the input / output of a pass between two dd passes is
@@ -684,6 +685,9 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         float4* o4 = reinterpret_cast<float4*>(out);
         if (i0 < nvalid) o4[off + (int64_t)i0 * a.out_st] = st_dd4(A);
         if (i1 < nvalid) o4[off + (int64_t)i1 * a.out_st] = st_dd4(B);
+      } else if (!IO::kDD && a.vec2 && i1 < nvalid) {  // lines 2q, 2q+1 in one 16-byte store
+        *reinterpret_cast<float4*>(out + off + i0) =
+            make_float4(outr<R>(A.re, 0), outr<R>(A.im, 0), outr<R>(B.re, 0), outr<R>(B.im, 0));
       } else {
         const int eo = line_emax_out(q);
         if (i0 < nvalid) {

@@ -706,6 +706,13 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.n_out = A.n_out;
   F.lmap_tile = A.in_tfast;
   F.out_tfast = A.out_tfast;
+  {  // float r2c: the split's two output lines in one 16-byte store (in the
+     // c2c kernel the same branch cost registers and spills, so it is r2c only)
+    bool v2 = P->rb == 4 && ps.op == OP_R2C && A.out_tfast && A.out_st == 1 &&
+              A.out_sa % 2 == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    for (int d = 0; d < A.nouter; ++d) v2 = v2 && A.out_so[d] % 2 == 0;
+    F.vec2 = v2 ? 1 : 0;
+  }
   F.store_direct = A.in_tfast ? A.out_tfast : (A.out_sa == 1 ? 1 : 0);
   F.in_dd = ps.in_dd ? 1 : 0;
   F.out_dd = ps.out_dd ? 1 : 0;
