@@ -72,7 +72,10 @@ def test_c3_taylor_green_mixed_512_512_257(cuda):
     assert rel(back, u) <= 1e-13
 
 
-def test_c4_rfft_1024_f32_properties(cuda):
+@pytest.mark.parametrize("precision", ["default", "tc"])
+def test_c4_rfft_1024_f32_properties(cuda, precision):
+    """C4 with the plain kernels and with the tensor-core split form (the
+    1024-point y and z lines as tcgen05 DFT-matrix products)."""
     import torch
     n = 1024
     dims = (n, n, n)
@@ -80,7 +83,7 @@ def test_c4_rfft_1024_f32_properties(cuda):
     amps = rng.uniform(1, 10, 8)
     phis = rng.uniform(0, 2 * np.pi, 8)
     ks = rng.integers(0, 64, size=(8, 3))
-    plan = P.PencilFFTPlan(dims, T.RFFT(), np.float32)
+    plan = P.PencilFFTPlan(dims, T.RFFT(), np.float32, precision=precision)
     A = plan.allocate_input()
     g = torch.Generator(device="cuda").manual_seed(1234)
     noise = torch.randn(A.data.shape, generator=g, device="cuda", dtype=torch.float32)
@@ -117,6 +120,7 @@ def test_c4_rfft_1024_f32_properties(cuda):
     B2.data[0, 0, 0] -= 3 * N
     diff = (B2.data - 2 * B.data).abs().double().norm().item() / (2 * B.data.abs().double().norm().item())
     assert diff <= 2e-6
+    assert plan.device_status() == 0
 
 
 def test_c5_vector_gradient_384(cuda):
