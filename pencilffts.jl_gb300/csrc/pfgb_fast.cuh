@@ -110,15 +110,23 @@ __device__ __forceinline__ Cx<R> mul_ik(Cx<R> y, int64_t idx, int half, int64_t 
 #ifndef PFGB_FAST_THREADS_DD
 #define PFGB_FAST_THREADS_DD 256
 #endif
+// float lines of 1024 points and more (c2c, r2c): CTAs of 1024 threads, so
+// that a tile still holds 8 lines (64-byte runs per position on strided
+// axes); measured on the 1024^3 Float32 round trip, y passes 2.45 -> 2.28 ms,
+// first backward pass 3.31 -> 2.79 ms.  c2r keeps 512 threads (at 1024 it
+// spills or runs one CTA per SM: 2.65 -> 3.42 ms).
+#ifndef PFGB_FAST_THREADS_F32_LONG
+#define PFGB_FAST_THREADS_F32_LONG 1024
+#endif
 template <typename R>
-__host__ __device__ constexpr int fast_threads(int logm) {
-  return sizeof(R) == 4 ? PFGB_FAST_THREADS_F32
+__host__ __device__ constexpr int fast_threads(int logm, int op = OP_C2C) {
+  return sizeof(R) == 4 ? (logm >= 10 && op != OP_C2R ? PFGB_FAST_THREADS_F32_LONG : PFGB_FAST_THREADS_F32)
                         : ((1 << logm) / 8 > PFGB_FAST_THREADS_DD ? (1 << logm) / 8 : PFGB_FAST_THREADS_DD);
 }
 // complex lines per CTA for a line of 2^logm points (one line at least)
 template <typename R>
-__host__ __device__ constexpr int fast_tw(int logm) {
-  return (fast_threads<R>(logm) * 8) >> logm > 0 ? ((fast_threads<R>(logm) * 8) >> logm) : 1;
+__host__ __device__ constexpr int fast_tw(int logm, int op = OP_C2C) {
+  return (fast_threads<R>(logm, op) * 8) >> logm > 0 ? ((fast_threads<R>(logm, op) * 8) >> logm) : 1;
 }
 // Shared-memory padding of the exchange buffer: one pad slot every 2^shift
 // elements plus `extra` slots per line.  Chosen from a bank model of the stage
@@ -133,13 +141,13 @@ __host__ __device__ constexpr int fast_pitch_extra(int tw, int ebytes) {
                       : (tw >= 16 ? 1 : tw == 8 ? 2 : tw == 4 ? 4 : tw == 2 ? 8 : 0);
 }
 template <typename R>
-__host__ __device__ constexpr int fast_pitch(int logm) {
+__host__ __device__ constexpr int fast_pitch(int logm, int op = OP_C2C) {
   return (1 << logm) + ((1 << logm) >> fast_pad_shift(logm, (int)sizeof(Cx<R>))) +
-         fast_pitch_extra(fast_tw<R>(logm), (int)sizeof(Cx<R>));
+         fast_pitch_extra(fast_tw<R>(logm, op), (int)sizeof(Cx<R>));
 }
 template <typename R>
-__host__ __device__ constexpr size_t fast_smem(int logm) {
-  return (size_t)fast_tw<R>(logm) * fast_pitch<R>(logm) * sizeof(Cx<R>);
+__host__ __device__ constexpr size_t fast_smem(int logm, int op = OP_C2C) {
+  return (size_t)fast_tw<R>(logm, op) * fast_pitch<R>(logm, op) * sizeof(Cx<R>);
 }
 
 template <typename R>
@@ -181,9 +189,9 @@ template <typename R, int LOGM>
 __host__ __device__ constexpr int padded(int pos) {
   return pos + (pos >> fast_pad_shift(LOGM, (int)sizeof(Cx<R>)));
 }
-template <typename R, int LOGM>
+template <typename R, int LOGM, int OP>
 __device__ __forceinline__ int sidx(int p, int pos) {
-  return p * fast_pitch<R>(LOGM) + padded<R, LOGM>(pos);
+  return p * fast_pitch<R>(LOGM, OP) + padded<R, LOGM>(pos);
 }
 // The padding is additive over the exchange patterns: with all sizes powers
 // of two, padded(p0 + r L) = padded(p0) + padded(r L) for 0 <= r < 8 when
@@ -197,10 +205,10 @@ __device__ __forceinline__ int sidx(int p, int pos) {
 // barrier per line (ids 1..lines, T a multiple of 32) or a warp barrier when
 // a warp holds whole lines.  With lines across the thread index (strided
 // axis, lanes along the tile dimension) every warp holds every line.
-template <typename R, int LOGM>
+template <typename R, int LOGM, int OP>
 __device__ __forceinline__ void line_sync(bool lanes_across_lines, int p) {
   constexpr int T = (1 << LOGM) / 8;
-  if (lanes_across_lines || T == fast_threads<R>(LOGM)) {
+  if (lanes_across_lines || T == fast_threads<R>(LOGM, OP)) {
     __syncthreads();
   } else if constexpr (T <= 32) {
     __syncwarp();
@@ -209,7 +217,7 @@ __device__ __forceinline__ void line_sync(bool lanes_across_lines, int p) {
   }
 }
 
-template <typename R, int LOGM, int SIGN>
+template <typename R, int LOGM, int SIGN, int OP>
 __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int b, const void* tw,
                                             bool lanes_across_lines) {
   constexpr int M = 1 << LOGM;
@@ -234,7 +242,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       }
       dft8<SIGN>(v);
       if (!last) {
-        Cx<R>* zw = z + sidx<R, LOGM>(p, (b - j) * 8 + j);
+        Cx<R>* zw = z + sidx<R, LOGM, OP>(p, (b - j) * 8 + j);
 #pragma unroll
         for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * Ls)] = v[r];
       }
@@ -260,11 +268,11 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       }
     }
     if (!last) {
-      line_sync<R, LOGM>(lanes_across_lines, p);
-      const Cx<R>* zr = z + sidx<R, LOGM>(p, b);
+      line_sync<R, LOGM, OP>(lanes_across_lines, p);
+      const Cx<R>* zr = z + sidx<R, LOGM, OP>(p, b);
 #pragma unroll
       for (int r = 0; r < 8; ++r) v[r] = zr[padded<R, LOGM>(r * T)];
-      line_sync<R, LOGM>(lanes_across_lines, p);
+      line_sync<R, LOGM, OP>(lanes_across_lines, p);
     }
   }
 }
@@ -324,9 +332,15 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 // kernel variant: operation OP and IOM = dd input (bit 0) | dd output (bit 1)
 template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
-  return sizeof(R) == 4 ? (op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS)
-         : fast_threads<R>(logm) >= 512 ? 1
-         : PFGB_FAST_DD_MINBLOCKS <= 0 ? 512 / fast_threads<R>(logm)
+  return sizeof(R) == 4
+             ? (op == OP_C2R && fast_threads<R>(logm, op) >= 1024
+                    ? 1  // c2r at 1024 threads spills heavily at 32 registers
+                    : ((op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS) <
+                               2048 / fast_threads<R>(logm, op)
+                           ? (op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS)
+                           : 2048 / fast_threads<R>(logm, op)))
+         : fast_threads<R>(logm, op) >= 512 ? 1
+         : PFGB_FAST_DD_MINBLOCKS <= 0 ? 512 / fast_threads<R>(logm, op)
          : (op == OP_C2R && !(iom & 1) && PFGB_FAST_DD_MINBLOCKS > 4) ? 4
                                                                      : PFGB_FAST_DD_MINBLOCKS;
 }
@@ -364,15 +378,15 @@ __device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bi
 // (self_scale): the largest biased exponent over the line (over the tile when
 // lines lie across the thread index).  The lines' leaders record it for the
 // next pass and fold it into the run's exponent word.  Called by all threads.
-template <typename R, int LOGM>
+template <typename R, int LOGM, int OP>
 __device__ __forceinline__ int line_exponent(unsigned emx, const FastArgs& a, unsigned bid, int64_t t0,
                                              int p, int nvalid_cl, bool lanes_across_lines) {
   constexpr int T = (1 << LOGM) / 8;
-  constexpr int TW = fast_tw<R>(LOGM);
+  constexpr int TW = fast_tw<R>(LOGM, OP);
   __shared__ unsigned wmax[32];
   unsigned e;
   bool leader;
-  if (lanes_across_lines || T == fast_threads<R>(LOGM)) {
+  if (lanes_across_lines || T == fast_threads<R>(LOGM, OP)) {
     emx = __reduce_max_sync(0xFFFFFFFFu, emx);
     const int nw = (blockDim.x + 31) >> 5;
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = emx;
@@ -396,8 +410,8 @@ __device__ __forceinline__ int line_exponent(unsigned emx, const FastArgs& a, un
   }
   // leader of line q: line p in the per-line branches, thread q in the
   // tile-wide branch (all lines share e)
-  const int q = (lanes_across_lines && !(T == fast_threads<R>(LOGM))) ? (int)threadIdx.x
-                : (T == fast_threads<R>(LOGM) ? 0 : p);
+  const int q = (lanes_across_lines && !(T == fast_threads<R>(LOGM, OP))) ? (int)threadIdx.x
+                : (T == fast_threads<R>(LOGM, OP) ? 0 : p);
   if (leader && q < nvalid_cl) {
     const int pk = a.op == OP_C2C ? 1 : 2;
     const unsigned rest = div31(bid, a.div_tiles);
@@ -441,7 +455,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   using MC = typename IO::MC;
   constexpr int M = 1 << LOGM;
   constexpr int T = M / 8;
-  constexpr int TW = fast_tw<R>(LOGM);
+  constexpr int TW = fast_tw<R>(LOGM, OP);
 
   const int tid = threadIdx.x;
   int p, b;
@@ -500,7 +514,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
           unsigned emx = 0;
 #pragma unroll
           for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
-          emax = line_exponent<R, LOGM>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
@@ -529,7 +543,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
         unsigned emx = 0;
 #pragma unroll
         for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
-        emax = line_exponent<R, LOGM>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+        emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
         emax_out = emax + a.emax_shift;
       }
     }
@@ -554,7 +568,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
 #pragma unroll
           for (int r = 0; r < 8; ++r)
             emx = max(emx, max(max(dexp_u(ra[r].x), dexp_u(ra[r].y)), max(dexp_u(rb[r].x), dexp_u(rb[r].y))));
-          emax = line_exponent<R, LOGM>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
@@ -591,7 +605,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
   if (IO::kDD && a.self_scale && b == 0) lexp[p] = emax;
 
   // ---- stages ----
-  fast_stages<R, LOGM, SIGN>(v, z, p, b, a.tw, a.lmap_tile != 0);
+  fast_stages<R, LOGM, SIGN, OP>(v, z, p, b, a.tw, a.lmap_tile != 0);
 
   // ---- store ----
   if (a.deriv == 2 && a.store_direct && OP == OP_C2C) {
@@ -636,7 +650,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
 
   // via shared memory: transposed layouts and the r2c split
   {
-    Cx<R>* zw = z + sidx<R, LOGM>(p, b);
+    Cx<R>* zw = z + sidx<R, LOGM, OP>(p, b);
 #pragma unroll
     for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * T)] = v[r];
   }
@@ -652,7 +666,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       int i, k;
       if (a.out_tfast) { i = e % TW; k = e / TW; } else { k = e % M; i = e / M; }
       if (i >= nvalid) continue;
-      Cx<R> y = apply_scale(z[sidx<R, LOGM>(i, k)], a);
+      Cx<R> y = apply_scale(z[sidx<R, LOGM, OP>(i, k)], a);
       if (a.deriv == 2) {
         const int64_t idx = a.deriv_role == 0 ? (int64_t)k : a.deriv_role == 1 ? t0 + i : didx;
         y = mul_ik(y, idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
@@ -674,8 +688,8 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
     for (int e = tid; e < tot; e += nth) {
       int q, k;
       if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % m; q = e / m; }
-      const Cx<R> f = z[sidx<R, LOGM>(q, k)];
-      const Cx<R> g = conj(z[sidx<R, LOGM>(q, k == 0 ? 0 : M - k)]);
+      const Cx<R> f = z[sidx<R, LOGM, OP>(q, k)];
+      const Cx<R> g = conj(z[sidx<R, LOGM, OP>(q, k == 0 ? 0 : M - k)]);
       Cx<R> A = f + g, B = mul_mi(f - g);
       A = apply_scale(mk(half(A.re), half(A.im)), a);
       B = apply_scale(mk(half(B.re), half(B.im)), a);
@@ -710,7 +724,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
     for (int e = tid; e < tot; e += nth) {
       int q, k;
       if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % M; q = e / M; }
-      const Cx<R> y = apply_scale(z[sidx<R, LOGM>(q, k)], a);
+      const Cx<R> y = apply_scale(z[sidx<R, LOGM, OP>(q, k)], a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
       const int eo = line_emax_out(q);
@@ -725,7 +739,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
 // registers (c2c at 64 registers: 8-16 bytes of spill against 96-140 bytes
 // with all three operations in one kernel).
 template <typename R, int LOGM, int SIGN, int OP, int IOM>
-__global__ void __launch_bounds__(fast_threads<R>(LOGM), fast_min_blocks<R>(LOGM, OP, IOM))
+__global__ void __launch_bounds__(fast_threads<R>(LOGM, OP), fast_min_blocks<R>(LOGM, OP, IOM))
     fast_pass(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   fast_tile<R, LOGM, SIGN, OP, IOM>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw), a.in, -1, a.in_sa, a.in_st);
@@ -785,18 +799,18 @@ __host__ __device__ constexpr int tma_line_bytes(int op) {
 }
 template <typename R, int LOGM>
 __host__ __device__ constexpr int tma_tile_bytes(int op) {
-  return ((op == OP_C2C ? fast_tw<R>(LOGM) : 2 * fast_tw<R>(LOGM)) * tma_line_bytes<R, LOGM>(op) + 127) /
+  return ((op == OP_C2C ? fast_tw<R>(LOGM, OP_C2R) : 2 * fast_tw<R>(LOGM, OP_C2R)) * tma_line_bytes<R, LOGM>(op) + 127) /
          128 * 128;
 }
 template <typename R, int LOGM>
 __host__ __device__ constexpr size_t tma_smem(int op) {
-  return (fast_smem<R>(LOGM) + 127) / 128 * 128 + 2 * (size_t)tma_tile_bytes<R, LOGM>(op);
+  return (fast_smem<R>(LOGM, OP_C2R) + 127) / 128 * 128 + 2 * (size_t)tma_tile_bytes<R, LOGM>(op);
 }
 
 template <typename R, int LOGM>
 __device__ __forceinline__ void tma_issue(const FastArgs& a, int64_t bid, unsigned char* buf,
                                           unsigned long long* bar) {
-  constexpr int TW = fast_tw<R>(LOGM);
+  constexpr int TW = fast_tw<R>(LOGM, OP_C2R);
   const int lines = a.op == OP_C2C ? TW : 2 * TW;
   const int lb = tma_line_bytes<R, LOGM>(a.op);
   const int esz = a.op == OP_R2C ? (int)sizeof(typename FastIO<R>::MR) : 2 * (int)sizeof(typename FastIO<R>::MR);
@@ -818,16 +832,16 @@ __device__ __forceinline__ void tma_issue(const FastArgs& a, int64_t bid, unsign
 
 template <typename R>
 __host__ __device__ constexpr int tma_min_blocks(int logm) {
-  return sizeof(R) == 4 ? 2 : (fast_threads<R>(logm) <= 256 ? 2 : 1);
+  return sizeof(R) == 4 ? 2 : (fast_threads<R>(logm, OP_C2R) <= 256 ? 2 : 1);
 }
 
 template <typename R, int LOGM, int SIGN, int IOM>
-__global__ void __launch_bounds__(fast_threads<R>(LOGM), tma_min_blocks<R>(LOGM)) fast_pass_tma(const FastArgs a) {
+__global__ void __launch_bounds__(fast_threads<R>(LOGM, OP_C2R), tma_min_blocks<R>(LOGM)) fast_pass_tma(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ int s_fail;
   Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
-  const size_t zb = (fast_smem<R>(LOGM) + 127) / 128 * 128;
+  const size_t zb = (fast_smem<R>(LOGM, OP_C2R) + 127) / 128 * 128;
   const int tb = tma_tile_bytes<R, LOGM>(a.op);
   unsigned char* buf0 = smem_raw + zb;
   const int line_elems = a.op == OP_C2R ? (1 << LOGM) / 2 + 1 : (1 << LOGM);

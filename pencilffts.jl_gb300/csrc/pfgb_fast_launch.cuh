@@ -19,10 +19,10 @@ int fail_cuda(cudaError_t e, const char* what);
 template <typename R, int LOGM, int SIGN, int OP, int IOM>
 static int launch_fast_one(const FastArgs& A, int64_t grid, cudaStream_t s) {
   static bool configured[kMaxDevicesConfigured] = {};
-  const size_t smem = fast_smem<R>(LOGM);
+  const size_t smem = fast_smem<R>(LOGM, OP);
   int rc = ensure_smem_attr(fast_pass<R, LOGM, SIGN, OP, IOM>, (int)smem, configured, "cudaFuncSetAttribute(fast_pass)");
   if (rc || grid == 0) return rc;
-  fast_pass<R, LOGM, SIGN, OP, IOM><<<(unsigned)grid, fast_threads<R>(LOGM), smem, s>>>(A);
+  fast_pass<R, LOGM, SIGN, OP, IOM><<<(unsigned)grid, fast_threads<R>(LOGM, OP), smem, s>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda(e, "fast_pass launch");
   return PFGB_OK;
@@ -65,13 +65,13 @@ static int launch_tma_one(const FastArgs& A, cudaStream_t s) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fast_pass_tma<R, LOGM, SIGN, IOM>,
-                                                                  fast_threads<R>(LOGM), smem);
+                                                                  fast_threads<R>(LOGM, OP_C2R), smem);
     if (e != cudaSuccess) return fail_cuda(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     max_grid[dev] = sms * (per_sm > 0 ? per_sm : 1);
   }
   if (A.total == 0) return PFGB_OK;
   const int64_t grid = A.total < max_grid[dev] ? A.total : max_grid[dev];
-  fast_pass_tma<R, LOGM, SIGN, IOM><<<(unsigned)grid, fast_threads<R>(LOGM), smem, s>>>(A);
+  fast_pass_tma<R, LOGM, SIGN, IOM><<<(unsigned)grid, fast_threads<R>(LOGM, OP_C2R), smem, s>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda(e, "fast_pass_tma launch");
   return PFGB_OK;

@@ -498,10 +498,10 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
     rc = upload_fast_table(P, M, &ps.ftw);
     if (rc) return rc;
     const bool packed = ps.op != OP_C2C;
-    ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm) : fast_tw<float>(ps.logm);
+    ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.op) : fast_tw<float>(ps.logm, ps.op);
     ps.lines = packed ? 2 * ps.clines : ps.clines;
-    ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm) : fast_threads<float>(ps.logm);
-    ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm) : fast_smem<float>(ps.logm);
+    ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm, ps.op) : fast_threads<float>(ps.logm, ps.op);
+    ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm, ps.op) : fast_smem<float>(ps.logm, ps.op);
     if (P->precision == PFGB_PRECISION_TC_SPLIT && ps.op == OP_C2C && tc_lines(ps.logm) > 0) {
       ps.tc = true;
       ps.clines = ps.lines = tc_lines(ps.logm);
