@@ -88,6 +88,20 @@ __device__ __forceinline__ int dexp_bits(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
+// Rare cases of d2dd and dd2d, out of line: inlined at every conversion
+// site they would only add instruction-cache footprint.
+static __device__ __noinline__ dd d2dd_rare(unsigned hi32, unsigned fs, int e, int c) {
+  const unsigned sign = hi32 & 0x80000000u;
+  const int ef = e + c;
+  if (e == 0x7FF) return dd(__uint_as_float(0x7FC00000u), 0.0f);
+  if (e == 0 || ef <= 0) return dd(0.0f, 0.0f);
+  return dd(__uint_as_float(sign | ((unsigned)ef << 23) | (fs & 0x7FFFFFu)), 0.0f);
+}
+static __device__ __noinline__ double dd2d_rare(unsigned sb, int es, int off) {
+  if (es == 255 || es + off >= 0x7FF) return __longlong_as_double(0x7FF8000000000000ll);
+  return __longlong_as_double((long long)((unsigned long long)(sb & 0x80000000u) << 32));
+}
+
 // x * 2^(1023 - emax) as dd.  hi keeps the top 24 significand bits of x, lo
 // the remaining 29 bits rounded to a float (I2F, then an exact power-of-two
 // scale).  emax is the largest biased exponent of the data being converted.
@@ -97,6 +111,7 @@ __device__ __forceinline__ int dexp_bits(double x) {
 // (e + 127 - emax) mod 512 = ef.  Rare cases: zero, subnormal and values
 // more than 2^126 below 2^(emax-1023) become zero, Inf/NaN become NaN, and
 // values 2^74..2^126 below keep hi only.
+
 __device__ __forceinline__ dd d2dd(double x, int emax) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
@@ -111,10 +126,7 @@ __device__ __forceinline__ dd d2dd(double x, int emax) {
     const float sc = __uint_as_float((hx & 0x7F800000u) - (52u << 23));  // 2^(ef - 179)
     return dd(__uint_as_float(hx | sign), __uint_as_float(__float_as_uint(__fmul_rn(r, sc)) | sign));
   }
-  const int ef = e + c;
-  if (e == 0x7FF) return dd(__uint_as_float(0x7FC00000u), 0.0f);
-  if (e == 0 || ef <= 0) return dd(0.0f, 0.0f);
-  return dd(__uint_as_float(sign | ((unsigned)ef << 23) | (fs & 0x7FFFFFu)), 0.0f);
+  return d2dd_rare(hi32, fs, e, c);
 }
 
 // (v.h + v.l) * 2^(emax - 1023) as a double, within one unit in the last
@@ -143,8 +155,7 @@ __device__ __forceinline__ double dd2d(dd v, int emax) {
     const unsigned long long bits = (((unsigned long long)hw << 32) | (sb << 29)) + (unsigned long long)(long long)li;
     return __longlong_as_double((long long)bits);
   }
-  if (es == 255 || es + off >= 0x7FF) return __longlong_as_double(0x7FF8000000000000ll);
-  return __longlong_as_double((long long)((unsigned long long)sign << 32));
+  return dd2d_rare(sb, es, off);
 }
 #endif
 
