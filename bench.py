@@ -38,7 +38,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--dims", default="512,512,512")
     ap.add_argument("--real", default="f64", choices=["f64", "f32"])
-    ap.add_argument("--precision", default="default", choices=["default", "native", "tc"])
+    ap.add_argument("--precision", default="default", choices=["default", "native", "fx", "tc"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",

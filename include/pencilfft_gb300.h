@@ -94,8 +94,20 @@ typedef struct pfgb_plan_desc {
  *             as two DFT-matrix products on the tensor cores (tf32 hi/lo
  *             split, three products, FP32 accumulation); other lines as in
  *             DEFAULT.  Relative L2 error about 1e-6 for a 3D round trip.
- *             The benchmark spec's precision form; FFTW has no such mode. */
-enum { PFGB_PRECISION_DEFAULT = 0, PFGB_PRECISION_NATIVE = 1, PFGB_PRECISION_TC_SPLIT = 2 };
+ *             The benchmark spec's precision form; FFTW has no such mode.
+ *   BLOCK_FLOAT: Float64 plans only: power-of-two c2c/r2c/c2r lines in block
+ *             floating point (64-bit integer components, one power-of-two
+ *             scale per line, 50 bits below each line's largest component
+ *             for 512-point lines, 47 at 4096; exact integer sums); executions
+ *             with a fused derivative use double-float.  Relative L2 error
+ *             about 2e-14 for a 512^3 round trip; on GB300 about 8% slower
+ *             than DEFAULT (the integer pipes run at half the FP32 rate). */
+enum {
+  PFGB_PRECISION_DEFAULT = 0,
+  PFGB_PRECISION_NATIVE = 1,
+  PFGB_PRECISION_TC_SPLIT = 2,
+  PFGB_PRECISION_BLOCK_FLOAT = 3
+};
 
 typedef struct pfgb_plan pfgb_plan;
 

@@ -11,16 +11,19 @@
 // write contiguous runs along either the line (axis-contiguous layouts) or
 // the tile dimension (axis-strided layouts).
 //
-// R is the arithmetic type: float, or dd (double-float on the FP32 pipes) for
-// Float64 data; dd data are scaled by powers of two (each line's largest
-// exponent in the first pass of a run, the run's largest afterwards) so that
-// any finite double range fits the float exponent range.
+// R is the arithmetic type: float for Float32 data; for Float64 data dd
+// (double-float on the FP32 pipes, the default) or fx (64-bit integers with
+// a per-line power-of-two scale, PFGB_PRECISION_BLOCK_FLOAT).  dd data are scaled by powers of two
+// (each line's largest exponent in the first pass of a run, the run's
+// largest afterwards) so that any finite double range fits the float
+// exponent range; fx lines carry their own scale from pass to pass.
 #pragma once
 
 #include <type_traits>
 
 #include "pfgb_dd.cuh"
 #include "pfgb_device.cuh"
+#include "pfgb_fx.cuh"
 
 namespace pfgb {
 
@@ -82,6 +85,13 @@ struct FastArgs {
   // tensor-core split form: the DFT matrices' tf32 hi / lo parts in the
   // shared-memory operand layout (tc_pass)
   const void* tcb;
+  // fx passes (R = fx): exponent words of the input lines (te_in, indexed as
+  // te above, present when the input is in fx form) and of the output lines
+  // (te_out, when the output is); the ldiv! normalisation's significand as
+  // round(m 2^60), m in [0.5, 1) (its exponent is in emax_shift)
+  const int* te_in;
+  int* te_out;
+  long long scale_fx;
 };
 
 // i k y for the frequency of index idx (fftfreq: idx - n above (n-1)/2,
@@ -158,12 +168,21 @@ struct FastIO<float> {
   using MR = float;
   using MC = float2;
   static constexpr bool kDD = false;
+  static constexpr bool kFX = false;
 };
 template <>
 struct FastIO<dd> {
   using MR = double;
   using MC = double2;
   static constexpr bool kDD = true;
+  static constexpr bool kFX = false;
+};
+template <>
+struct FastIO<fx> {
+  using MR = double;
+  using MC = double2;
+  static constexpr bool kDD = false;
+  static constexpr bool kFX = true;
 };
 
 template <typename R>
@@ -180,7 +199,23 @@ __device__ __forceinline__ Cx<R> ldg_tw(const void* t, int m) {
 template <typename R>
 __device__ __forceinline__ R half(R x) {
   if constexpr (std::is_same<R, dd>::value) return dd(x.h * 0.5f, x.l * 0.5f);
+  else if constexpr (std::is_same<R, fx>::value) return fx(x.v >> 1);
   else return x * 0.5f;
+}
+
+// v * exp(SIGN 2 pi i m / M) from the pass's twiddle table (fx tables hold
+// the pass's sign already)
+template <typename R, int SIGN>
+__device__ __forceinline__ Cx<R> tw_mul(Cx<R> v, const void* tw, int m) {
+  if constexpr (std::is_same<R, fx>::value) {
+    const int4 q = __ldg(reinterpret_cast<const int4*>(tw) + m);
+    fx_twiddle(v.re, v.im, fx_tw{q.x, q.y, q.z, q.w});
+    return v;
+  } else {
+    Cx<R> w = ldg_tw<R>(tw, m);
+    if (SIGN > 0) w = conj(w);
+    return v * w;
+  }
 }
 
 // Shared-memory slot of element pos of complex line p (padding avoids bank
@@ -234,11 +269,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       if (Ls > 1) {
         const int step = j * (M / (8 * Ls));
 #pragma unroll
-        for (int r = 1; r < 8; ++r) {
-          Cx<R> w = ldg_tw<R>(tw, r * step);
-          if (SIGN > 0) w = conj(w);
-          v[r] = v[r] * w;
-        }
+        for (int r = 1; r < 8; ++r) v[r] = tw_mul<R, SIGN>(v[r], tw, r * step);
       }
       dft8<SIGN>(v);
       if (!last) {
@@ -255,11 +286,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
       for (int r1 = 0; r1 < G; ++r1) {
         const int beta = b + r1 * T;
 #pragma unroll
-        for (int q = 1; q < RS; ++q) {
-          Cx<R> w = ldg_tw<R>(tw, q * beta);
-          if (SIGN > 0) w = conj(w);
-          v[r1 + q * G] = v[r1 + q * G] * w;
-        }
+        for (int q = 1; q < RS; ++q) v[r1 + q * G] = tw_mul<R, SIGN>(v[r1 + q * G], tw, q * beta);
         if constexpr (RS == 2) {
           dft2<SIGN>(v[r1], v[r1 + G]);
         } else {
@@ -303,7 +330,10 @@ __device__ __forceinline__ float4 st_dd4(Cx<R> y) {
 template <typename R>
 __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
   if (!a.scale_on) return y;
-  if constexpr (std::is_same<R, dd>::value) {
+  if constexpr (std::is_same<R, fx>::value) {
+    const fx s(a.scale_fx);
+    return mk(y.re * s, y.im * s);
+  } else if constexpr (std::is_same<R, dd>::value) {
     const dd s(a.scale_h, a.scale_l);
     return mk(y.re * s, y.im * s);
   } else {
@@ -446,8 +476,8 @@ __device__ __forceinline__ Cx<R> scale_pow2(Cx<R> y, float f) {
 // is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
 // offset in the pass input).
 template <typename R, int LOGM, int SIGN, int OP, int IOM>
-__device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
-                                          int64_t soff, int64_t ssa, int64_t sst) {
+__device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
+                                              int64_t soff, int64_t ssa, int64_t sst) {
   using IO = FastIO<R>;
   constexpr bool IN_DD = IO::kDD && (IOM & 1) != 0;   // input in dd form
   constexpr bool OUT_DD = IO::kDD && (IOM & 2) != 0;  // output in dd form
@@ -732,6 +762,305 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>*
       if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
     }
   }
+}
+
+// One tile of an fx pass (R = fx).  Load: each complex line gets the scale
+// 2^(et - H), et its largest exponent (values below 2^et): from the doubles'
+// exponents, or from the exponent words of the fx lines its elements come
+// from, each element shifted to the line's scale.  Store: double outputs are
+// converted from the line's scale; fx outputs are shifted so that the line's
+// largest component reaches bit 61 (bit length by a per-line OR), and the
+// line's exponent word is recorded for the next pass.
+template <int LOGM, int SIGN, int OP, int IOM>
+__device__ __forceinline__ void fast_tile_fx(const FastArgs& a, int64_t bid, Cx<fx>* z, const void* src,
+                                             int64_t soff, int64_t ssa, int64_t sst) {
+  constexpr bool IN_FX = (IOM & 1) != 0;
+  constexpr bool OUT_FX = (IOM & 2) != 0;
+  constexpr int M = 1 << LOGM;
+  constexpr int T = M / 8;
+  constexpr int TW = fast_tw<fx>(LOGM, OP);
+  constexpr int H = fx_head(LOGM, OP == OP_C2R);
+
+  const int tid = threadIdx.x;
+  int p, b;
+  if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
+  const bool packed = OP != OP_C2C;
+  const int lines = packed ? 2 * TW : TW;
+  const TileOrigin o = tile_origin(a, (unsigned)bid, lines);
+  const int64_t t0 = o.t0, ooff = o.ooff;
+  const int64_t ioff = soff >= 0 ? soff : o.ioff;
+  const int nvalid = (int)min((int64_t)lines, a.nt - t0);
+  const int ncl_valid = packed ? (nvalid + 1) / 2 : nvalid;
+
+  // per complex line: [0] largest input exponent (biased double exponent, or
+  // the largest exponent word), [1] bit length of the output components
+  __shared__ int red[2][TW];
+  if (tid < TW) {
+    red[0][tid] = kTeZero;
+    red[1][tid] = 0;
+  }
+  __syncthreads();
+  // largest exponent et of complex line i (values below 2^et)
+  auto line_et = [&](int i) {
+    const int x = red[0][i];
+    return IN_FX ? x : (x == 0x7FF ? kTeNaN : x - 1022);
+  };
+
+  Cx<fx> v[8];
+  if constexpr (OP == OP_C2C) {
+    if constexpr (IN_FX) {
+      const longlong2* in = reinterpret_cast<const longlong2*>(src) + ioff + (int64_t)p * sst;
+      longlong2 q[8];
+      int tev[8];
+      int tm = kTeZero;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const bool ok = p < nvalid;
+        q[r] = ok ? in[(int64_t)(b + r * T) * ssa] : make_longlong2(0, 0);
+        tev[r] = ok ? __ldg(a.te_in + te_index(a, o.tebase, t0 + p, b + r * T)) : kTeZero;
+        tm = max(tm, tev[r]);
+      }
+      atomicMax(&red[0][p], tm);
+      __syncthreads();
+      const int sb = red[0][p] - H + 61;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = mk(fx(fx_shr(q[r].x, sb - tev[r])), fx(fx_shr(q[r].y, sb - tev[r])));
+    } else {
+      const double2* in = reinterpret_cast<const double2*>(src) + ioff + (int64_t)p * sst;
+      double2 raw[8];
+      unsigned emx = 0;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        raw[r] = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : make_double2(0.0, 0.0);
+        emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
+      }
+      atomicMax(&red[0][p], (int)emx);
+      __syncthreads();
+      const int base = red[0][p] + 53 - H;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = mk(fx(d2fx(raw[r].x, base)), fx(d2fx(raw[r].y, base)));
+    }
+  } else if constexpr (OP == OP_R2C) {
+    // two real lines (2p, 2p+1) as one complex line; always double input
+    const double* in = reinterpret_cast<const double*>(src) + ioff;
+    const int i0 = 2 * p, i1 = 2 * p + 1;
+    double ra[8], rb[8];
+    unsigned emx = 0;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int64_t off = (int64_t)(b + r * T) * ssa;
+      ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : 0.0;
+      rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : 0.0;
+      emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
+    }
+    atomicMax(&red[0][p], (int)emx);
+    __syncthreads();
+    const int base = red[0][p] + 53 - H;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = mk(fx(d2fx(ra[r], base)), fx(d2fx(rb[r], base)));
+  } else {  // OP_C2R: Hermitian extension of two half spectra, n = M, m = n_in
+    // exponents first (input lines' words, or the doubles' exponents), then
+    // load, convert and combine after the line's scale is known (the second
+    // reads hit L1); holding the raw values across the barrier would spill
+    const int m = a.n_in;
+    const int i0 = 2 * p, i1 = 2 * p + 1;
+    int tm = kTeZero;
+    unsigned emx = 0;
+    int ta[8], tb[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int pos = b + r * T;
+      const int k = pos < m ? pos : M - pos;
+      if constexpr (IN_FX) {
+        ta[r] = i0 < nvalid ? __ldg(a.te_in + te_index(a, o.tebase, t0 + i0, k)) : kTeZero;
+        tb[r] = i1 < nvalid ? __ldg(a.te_in + te_index(a, o.tebase, t0 + i1, k)) : kTeZero;
+        tm = max(tm, max(ta[r], tb[r]));
+      } else {
+        const double2* in = reinterpret_cast<const double2*>(src) + ioff;
+        const int64_t off = (int64_t)k * ssa;
+        const double2 qa = i0 < nvalid ? in[off + (int64_t)i0 * sst] : make_double2(0.0, 0.0);
+        const double2 qb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : make_double2(0.0, 0.0);
+        emx = max(emx, max(max(dexp_u(qa.x), dexp_u(qa.y)), max(dexp_u(qb.x), dexp_u(qb.y))));
+      }
+    }
+    atomicMax(&red[0][p], IN_FX ? tm : (int)emx);
+    __syncthreads();
+    const int sb = red[0][p] - H + 61;      // fx input: shift base
+    const int base = red[0][p] + 53 - H;   // double input: conversion base
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int pos = b + r * T;
+      const int k = pos < m ? pos : M - pos;
+      const int64_t off = (int64_t)k * ssa;
+      Cx<fx> A, B;
+      if constexpr (IN_FX) {
+        const longlong2* in = reinterpret_cast<const longlong2*>(src) + ioff;
+        const longlong2 qa = i0 < nvalid ? in[off + (int64_t)i0 * sst] : make_longlong2(0, 0);
+        const longlong2 qb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : make_longlong2(0, 0);
+        A = mk(fx(fx_shr(qa.x, sb - ta[r])), fx(fx_shr(qa.y, sb - ta[r])));
+        B = mk(fx(fx_shr(qb.x, sb - tb[r])), fx(fx_shr(qb.y, sb - tb[r])));
+      } else {
+        const double2* in = reinterpret_cast<const double2*>(src) + ioff;
+        const double2 qa = i0 < nvalid ? in[off + (int64_t)i0 * sst] : make_double2(0.0, 0.0);
+        const double2 qb = i1 < nvalid ? in[off + (int64_t)i1 * sst] : make_double2(0.0, 0.0);
+        A = mk(fx(d2fx(qa.x, base)), fx(d2fx(qa.y, base)));
+        B = mk(fx(d2fx(qb.x, base)), fx(d2fx(qb.y, base)));
+      }
+      if (k == 0 || 2 * k == M) { A.im = fx(0); B.im = fx(0); }
+      // pos < m: A + iB ; else conj(A) + i conj(B)
+      if (pos >= m) { A.im = -A.im; B.im = -B.im; }
+      v[r] = mk(A.re - B.im, A.im + B.re);
+    }
+  }
+
+  // ---- stages ----
+  fast_stages<fx, LOGM, SIGN, OP>(v, z, p, b, a.tw, a.lmap_tile != 0);
+
+  // ---- store ----
+  // exponent word of complex line i of the output (the line's scale is
+  // 2^(et - H); shifted left by 61 - bl its values lie below 2^(et - H + bl))
+  auto te_word = [&](int i) {
+    const int et = line_et(i), bl = red[1][i];
+    return et >= kTeNaN ? kTeNaN : bl == 0 ? kTeZero : et - H + bl;
+  };
+  // scale exponent of complex line i for double outputs
+  auto out_shift = [&](int i) { return line_et(i) - H + a.emax_shift; };
+  auto out_nan = [&](int i) { return line_et(i) >= kTeNaN; };
+  if constexpr (OUT_FX) {
+    unsigned long long orv = 0;
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+      orv |= (unsigned long long)(v[r].re.v ^ (v[r].re.v >> 63)) | (unsigned long long)(v[r].im.v ^ (v[r].im.v >> 63));
+    const int bl = orv ? 64 - __clzll((long long)orv) : 0;
+    atomicMax(&red[1][p], bl);
+  }
+  const double qnan = __longlong_as_double(0x7FF8000000000000ll);
+  if (a.store_direct && OP != OP_R2C) {
+    if constexpr (OP == OP_C2C) {
+      if constexpr (OUT_FX) {
+        __syncthreads();
+        const int sh = 61 - red[1][p];
+        if (p < nvalid) {
+          longlong2* out = reinterpret_cast<longlong2*>(a.out) + ooff + (int64_t)p * a.out_st;
+#pragma unroll
+          for (int r = 0; r < 8; ++r)
+            out[(int64_t)(b + r * T) * a.out_sa] = make_longlong2(v[r].re.v << sh, v[r].im.v << sh);
+        }
+      } else {
+        const int so = out_shift(p);
+        const bool nan = out_nan(p);
+        if (p < nvalid) {
+          double2* out = reinterpret_cast<double2*>(a.out) + ooff + (int64_t)p * a.out_st;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const Cx<fx> y = apply_scale(v[r], a);
+            out[(int64_t)(b + r * T) * a.out_sa] =
+                nan ? make_double2(qnan, qnan) : make_double2(fx2d(y.re.v, so), fx2d(y.im.v, so));
+          }
+        }
+      }
+    } else {  // C2R, real outputs of lines 2p and 2p+1
+      double* out = reinterpret_cast<double*>(a.out) + ooff;
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      const int so = out_shift(p);
+      const bool nan = out_nan(p);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const Cx<fx> y = apply_scale(v[r], a);
+        const int64_t off = (int64_t)(b + r * T) * a.out_sa;
+        if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = nan ? qnan : fx2d(y.re.v, so);
+        if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = nan ? qnan : fx2d(y.im.v, so);
+      }
+    }
+    if constexpr (OUT_FX) {
+      if (b == 0 && p < ncl_valid)
+        a.te_out[t0 / (packed ? 2 : 1) + p + a.te_ncl * div31((unsigned)bid, a.div_tiles)] = te_word(p);
+    }
+    return;
+  }
+
+  // via shared memory: transposed layouts and the r2c split
+  {
+    Cx<fx>* zw = z + sidx<fx, LOGM, OP>(p, b);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) zw[padded<fx, LOGM>(r * T)] = v[r];
+  }
+  __syncthreads();
+  if constexpr (OUT_FX) {
+    if (b == 0 && p < ncl_valid)
+      a.te_out[t0 / (packed ? 2 : 1) + p + a.te_ncl * div31((unsigned)bid, a.div_tiles)] = te_word(p);
+  }
+  const int nth = blockDim.x;
+  if constexpr (OP == OP_C2C) {
+    const int tot = TW * M;
+    for (int e = tid; e < tot; e += nth) {
+      int i, k;
+      if (a.out_tfast) { i = e % TW; k = e / TW; } else { k = e % M; i = e / M; }
+      if (i >= nvalid) continue;
+      const Cx<fx> y = z[sidx<fx, LOGM, OP>(i, k)];
+      const int64_t off = (int64_t)k * a.out_sa + (int64_t)i * a.out_st;
+      if constexpr (OUT_FX) {
+        const int sh = 61 - red[1][i];
+        reinterpret_cast<longlong2*>(a.out)[ooff + off] = make_longlong2(y.re.v << sh, y.im.v << sh);
+      } else {
+        const Cx<fx> ys = apply_scale(y, a);
+        const int so = out_shift(i);
+        reinterpret_cast<double2*>(a.out)[ooff + off] =
+            out_nan(i) ? make_double2(qnan, qnan) : make_double2(fx2d(ys.re.v, so), fx2d(ys.im.v, so));
+      }
+    }
+  } else if constexpr (OP == OP_R2C) {
+    const int m = a.n_out;
+    const int tot = TW * m;
+    for (int e = tid; e < tot; e += nth) {
+      int q, k;
+      if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % m; q = e / m; }
+      const Cx<fx> f = z[sidx<fx, LOGM, OP>(q, k)];
+      const Cx<fx> g = conj(z[sidx<fx, LOGM, OP>(q, k == 0 ? 0 : M - k)]);
+      Cx<fx> A = f + g, B = mul_mi(f - g);
+      A = mk(half(A.re), half(A.im));
+      B = mk(half(B.re), half(B.im));
+      const int i0 = 2 * q, i1 = 2 * q + 1;
+      const int64_t off = (int64_t)k * a.out_sa;
+      if constexpr (OUT_FX) {
+        const int sh = 61 - red[1][q];
+        longlong2* o2 = reinterpret_cast<longlong2*>(a.out) + ooff;
+        if (i0 < nvalid) o2[off + (int64_t)i0 * a.out_st] = make_longlong2(A.re.v << sh, A.im.v << sh);
+        if (i1 < nvalid) o2[off + (int64_t)i1 * a.out_st] = make_longlong2(B.re.v << sh, B.im.v << sh);
+      } else {
+        A = apply_scale(A, a);
+        B = apply_scale(B, a);
+        const int so = out_shift(q);
+        const bool nan = out_nan(q);
+        double2* o2 = reinterpret_cast<double2*>(a.out) + ooff;
+        if (i0 < nvalid)
+          o2[off + (int64_t)i0 * a.out_st] = nan ? make_double2(qnan, qnan) : make_double2(fx2d(A.re.v, so), fx2d(A.im.v, so));
+        if (i1 < nvalid)
+          o2[off + (int64_t)i1 * a.out_st] = nan ? make_double2(qnan, qnan) : make_double2(fx2d(B.re.v, so), fx2d(B.im.v, so));
+      }
+    }
+  } else {  // C2R with a transposed output layout
+    double* out = reinterpret_cast<double*>(a.out) + ooff;
+    const int tot = TW * M;
+    for (int e = tid; e < tot; e += nth) {
+      int q, k;
+      if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % M; q = e / M; }
+      const Cx<fx> y = apply_scale(z[sidx<fx, LOGM, OP>(q, k)], a);
+      const int i0 = 2 * q, i1 = 2 * q + 1;
+      const int64_t off = (int64_t)k * a.out_sa;
+      const int so = out_shift(q);
+      const bool nan = out_nan(q);
+      if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = nan ? qnan : fx2d(y.re.v, so);
+      if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = nan ? qnan : fx2d(y.im.v, so);
+    }
+  }
+}
+
+template <typename R, int LOGM, int SIGN, int OP, int IOM>
+__device__ __forceinline__ void fast_tile(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
+                                          int64_t soff, int64_t ssa, int64_t sst) {
+  if constexpr (FastIO<R>::kFX) fast_tile_fx<LOGM, SIGN, OP, IOM>(a, bid, z, src, soff, ssa, sst);
+  else fast_tile_std<R, LOGM, SIGN, OP, IOM>(a, bid, z, src, soff, ssa, sst);
 }
 
 // One kernel per variant (operation c2c / r2c / c2r, dd or double input and

@@ -116,7 +116,8 @@ struct Pass {
   int te_sh[2 + kMaxOuter] = {};
   unsigned te_mul[2 + kMaxOuter] = {};
   int logm = 0;
-  const void* ftw = nullptr;  // its twiddle table (float or dd entries)
+  const void* ftw = nullptr;     // its twiddle table (float or dd entries)
+  const void* ftw_fx = nullptr;  // Float64 plans: fx entries with the pass's sign
   // kernel variant chosen by the planner's measurement (autotune): -1
   // default, 0 plain fast_pass, 1 TMA-fed persistent form (c2r passes)
   int variant = -1;
@@ -168,6 +169,13 @@ struct pfgb_plan {
   std::map<std::string, void*> tables;
   int* emax_dev = nullptr;  // scale exponent of the current run of dd passes
   int* te_dev = nullptr;    // per-tile exponents of a run's first pass
+  // Float64 plans in block floating point (PFGB_PRECISION_BLOCK_FLOAT): fast
+  // passes in fx arithmetic (executions with a fused derivative use dd), and
+  // the exponent words of
+  // the lines passed between consecutive fast passes (pass i writes
+  // te_fx[i & 1])
+  bool fx = false;
+  int* te_fx[2] = {nullptr, nullptr};
   int device = 0;
   bool query_only = false;  // plan analysed on the host only (no device memory)
   // opt-in per-launch timing: (direction, pass index, start, stop)
@@ -313,6 +321,41 @@ static int upload_fast_table(pfgb_plan* P, int M, const void** out) {
   void* d = nullptr;
   PFGB_CUDA(cudaMalloc(&d, h.size() * sizeof(float)));
   PFGB_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  P->tables[key] = d;
+  *out = d;
+  return PFGB_OK;
+}
+
+// Twiddles of the fast kernel in fx form: exp(sign 2 pi i m / M) as
+// W = round(w 2^60) (clamped below 2^60) per part, stored as
+// (4 * (W >> 31), W & (2^31 - 1)) for the real and imaginary parts.
+static int upload_fast_table_fx(pfgb_plan* P, int M, int sign, const void** out) {
+  if (P->query_only) {
+    *out = nullptr;
+    return PFGB_OK;
+  }
+  const std::string key = "ftwfx" + std::to_string(sign) + "_" + std::to_string(M);
+  auto it = P->tables.find(key);
+  if (it != P->tables.end()) {
+    *out = it->second;
+    return PFGB_OK;
+  }
+  std::vector<int32_t> h;
+  h.reserve((size_t)M * 4);
+  const ld two60 = std::ldexp((ld)1, 60);
+  for (int m = 0; m < M; ++m) {
+    const std::complex<ld> w = expi_pi(2 * (int64_t)m * (sign < 0 ? 1 : -1), M);
+    for (ld c : {w.real(), w.imag()}) {
+      long long W = (long long)std::llround(c * two60);
+      if (W > (1ll << 60) - 1) W = (1ll << 60) - 1;
+      if (W < -(1ll << 60)) W = -(1ll << 60);
+      h.push_back((int32_t)(4 * (W >> 31)));
+      h.push_back((int32_t)(W & 0x7FFFFFFFll));
+    }
+  }
+  void* d = nullptr;
+  PFGB_CUDA(cudaMalloc(&d, h.size() * sizeof(int32_t)));
+  PFGB_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   P->tables[key] = d;
   *out = d;
   return PFGB_OK;
@@ -496,6 +539,7 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
     ps.logm = 0;
     while ((1 << ps.logm) < M) ++ps.logm;
     rc = upload_fast_table(P, M, &ps.ftw);
+    if (!rc && P->fx) rc = upload_fast_table_fx(P, M, ps.sign, &ps.ftw_fx);
     if (rc) return rc;
     const bool packed = ps.op != OP_C2C;
     ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.op) : fast_tw<float>(ps.logm, ps.op);
@@ -692,8 +736,11 @@ static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* o
   return PFGB_OK;
 }
 
+// fxi: index of the pass in its direction for fx arithmetic (selects the
+// exponent-word buffers), -1 for float / dd.
 static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, void* out,
-                          bool scale_on, FastArgs& F, int64_t& grid, const Deriv* dv = nullptr) {
+                          bool scale_on, FastArgs& F, int64_t& grid, const Deriv* dv = nullptr,
+                          int fxi = -1) {
   PassArgs A;
   int rc = make_args(P, ps, in, out, scale_on, A, grid, dv);
   if (rc) return rc;
@@ -732,10 +779,23 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   if (F.scale_on && P->rb == 8 && !ps.out_dd) {
     // a power-of-two normalisation of double outputs is an exponent offset
     int k = 0;
-    if (frexpl(sc, &k) == 0.5L) {
+    const ld mant = frexpl(sc, &k);
+    if (mant == 0.5L) {
       F.scale_on = 0;
       F.emax_shift = k - 1;
+    } else if (fxi >= 0) {
+      // fx: multiply by the significand, add the exponent at the conversion
+      F.scale_fx = (long long)llroundl(mant * std::ldexp((ld)1, 60));
+      F.emax_shift = k;
     }
+  }
+  if (fxi >= 0) {
+    F.tw = ps.ftw_fx;
+    F.te_in = ps.in_dd ? P->te_fx[(fxi + 1) & 1] : nullptr;
+    F.te_out = ps.out_dd ? P->te_fx[fxi & 1] : nullptr;
+    F.self_scale = 0;
+    F.te_rescale = 0;
+    F.te = nullptr;
   }
   F.deriv = A.deriv;
   F.deriv_role = A.deriv_role;
@@ -785,6 +845,7 @@ int launch_pass(int real_bytes, const PassArgs& A, int64_t grid, int threads, si
 int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_fx(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_emax(const void* x, int64_t n, int* out, cudaStream_t s);
 int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_tc(int logm, int sign, const FastArgs& A, cudaStream_t s);
@@ -1047,6 +1108,8 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       if (first_tr < 0) first_tr = i;
     }
   const int dpass = dv && dv->mode ? (dv->mode == 2 ? last_tr : first_tr) : -1;
+  // Float64 fast passes: fx, or dd for an execution with a fused derivative
+  const bool fxrun = P->fx && !(dv && dv->mode);
   if (dv && dv->mode) {
     if (dpass < 0 || dir.passes[dpass].op != OP_C2C)
       return fail(PFGB_ERR_UNSUPPORTED, "the fused derivative needs a complex-to-complex pass at that end "
@@ -1082,9 +1145,12 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
     } else if (ps.fast) {
       FastArgs F;
       int64_t grid = 0;
-      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr);
+      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr,
+                              fxrun ? i : -1);
       if (rc) return rc;
-      if (ps.tc) {
+      if (fxrun) {
+        rc = launch_fast_fx(ps.logm, ps.sign, F, grid, s);
+      } else if (ps.tc) {
         F.total = grid;
         F.err = P->emax_dev + 1;
         F.tcb = ps.tcb;
@@ -1150,10 +1216,12 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   if (d.real_bytes != 4 && d.real_bytes != 8)
     return fail(PFGB_ERR_ARGUMENT, "real type must be Float32 (4) or Float64 (8)");
   if (d.precision_mode != PFGB_PRECISION_DEFAULT && d.precision_mode != PFGB_PRECISION_NATIVE &&
-      d.precision_mode != PFGB_PRECISION_TC_SPLIT)
+      d.precision_mode != PFGB_PRECISION_TC_SPLIT && d.precision_mode != PFGB_PRECISION_BLOCK_FLOAT)
     return fail(PFGB_ERR_ARGUMENT, "unknown precision mode");
   if (d.precision_mode == PFGB_PRECISION_TC_SPLIT && d.real_bytes != 4)
     return fail(PFGB_ERR_ARGUMENT, "the tensor-core split form applies to Float32 plans");
+  if (d.precision_mode == PFGB_PRECISION_BLOCK_FLOAT && d.real_bytes != 8)
+    return fail(PFGB_ERR_ARGUMENT, "the block floating point form applies to Float64 plans");
   for (int n = 0; n < d.ndims; ++n) {
     if (d.dims[n] < 1) return fail(PFGB_ERR_ARGUMENT, "dimensions must be positive");
     if (d.kind[n] < PFGB_FFT || d.kind[n] > PFGB_NOTRANSFORM)
@@ -1176,6 +1244,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   P->D = P->N + P->K;
   P->rb = d.real_bytes;
   P->precision = d.precision_mode;
+  P->fx = d.real_bytes == 8 && d.precision_mode == PFGB_PRECISION_BLOCK_FLOAT;
   P->inplace = d.inplace[0] != 0;
   P->permute = d.permute_dims != 0;
   if (!query_only) cudaGetDevice(&P->device);
@@ -1252,8 +1321,8 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   for (auto* dir : {&P->fwd, &P->bwd})
     for (auto& ps : dir->passes)
       if (!rc) rc = prepare_pass(P, ps);
-  // Float64 runs of consecutive fast passes exchange data in dd form
-  int64_t te_tiles = 0;
+  // Float64 runs of consecutive fast passes exchange data in dd (or fx) form
+  int64_t te_tiles = 0, fx_lines = 0;
   if (!rc && P->rb == 8) {
     for (auto* dir : {&P->fwd, &P->bwd}) {
       auto& v = dir->passes;
@@ -1266,10 +1335,16 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
         v[i].reduce_before = !prev;
         v[i].self_scale = !prev;
       }
+      // element -> previous-pass line maps: the second pass of a dd run
+      // (te_rescale) and every pass of an fx run with fx input
       for (size_t i = 0; i + 1 < v.size(); ++i)
-        if (v[i].self_scale && v[i].out_dd) {
-          v[i + 1].te_rescale = true;
-          te_tiles = std::max(te_tiles, te_mapping(v[i], v[i + 1]));
+        if (v[i].out_dd) {
+          const int64_t n = te_mapping(v[i], v[i + 1]);
+          if (v[i].self_scale) {
+            v[i + 1].te_rescale = true;
+            te_tiles = std::max(te_tiles, n);
+          }
+          fx_lines = std::max(fx_lines, n);
         }
     }
   }
@@ -1287,6 +1362,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
           F.out_dd = ps.out_dd ? 1 : 0;
           rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
                           : launch_fast_f32(ps.logm, ps.sign, F, 0, nullptr);
+          if (!rc && P->fx) rc = launch_fast_fx(ps.logm, ps.sign, F, 0, nullptr);
           if (!rc && PFGB_FAST_TMA)
             rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
                             : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);
@@ -1301,6 +1377,10 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   }
   if (!rc && !query_only && te_tiles > 0) {
     cudaError_t e = cudaMalloc(&P->te_dev, (size_t)te_tiles * sizeof(int));
+    if (e != cudaSuccess) rc = fail(PFGB_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  for (int i = 0; i < 2 && !rc && !query_only && P->fx && fx_lines > 0; ++i) {
+    cudaError_t e = cudaMalloc(&P->te_fx[i], (size_t)fx_lines * sizeof(int));
     if (e != cudaSuccess) rc = fail(PFGB_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   }
   // exponent word (Float64 runs) and error word of the TMA-fed passes
@@ -1362,13 +1442,14 @@ int pfgb_plan_set_timing(pfgb_plan* P, int on) {
 // Planner measurement (desc.autotune; the reference's FFTW.MEASURE planning
 // flag): every pass with alternative kernels runs each of them on temporary
 // buffers filled with normal numbers (bytes 0x3F), and the faster is kept.
-// Alternatives today: c2r passes, plain fast_pass or the TMA-fed persistent
-// form (when the buffers satisfy its alignment).
+// Alternatives today: c2r passes of Float32 and double-float plans, plain
+// fast_pass or the TMA-fed persistent form (when the buffers satisfy its
+// alignment).
 static int autotune_passes(pfgb_plan* P) {
   const int e1023 = 1023;
   for (auto* dir : {&P->fwd, &P->bwd}) {
     for (auto& ps : dir->passes) {
-      if (!ps.fast || ps.op != OP_C2R || ps.tc) continue;
+      if (!ps.fast || ps.op != OP_C2R || ps.tc || P->fx) continue;  // fx passes have one kernel
       void* bin = nullptr;
       void* bout = nullptr;
       const size_t nin = (size_t)ps.lin.bytes(), nout = (size_t)ps.lout.bytes();
@@ -1450,7 +1531,7 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     const char* kname = ps.pk == PK_COPY ? "copy_kernel"
                         : ps.tc ? "tc_pass<tf32x3>"
                         : ps.variant == 1 ? (P->rb == 8 ? "fast_pass_tma<dd>" : "fast_pass_tma<float>")
-                        : ps.fast ? (P->rb == 8 ? "fast_pass<dd>" : "fast_pass<float>")
+                        : ps.fast ? (P->rb == 4 ? "fast_pass<float>" : P->fx ? "fast_pass<fx>" : "fast_pass<dd>")
                                   : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);
     acc.push_back(e);
@@ -1478,6 +1559,8 @@ int pfgb_plan_destroy(pfgb_plan* P) {
   for (auto& kv : P->tables) cudaFree(kv.second);
   if (P->emax_dev) cudaFree(P->emax_dev);
   if (P->te_dev) cudaFree(P->te_dev);
+  for (int i = 0; i < 2; ++i)
+    if (P->te_fx[i]) cudaFree(P->te_fx[i]);
   delete P;
   return PFGB_OK;
 }

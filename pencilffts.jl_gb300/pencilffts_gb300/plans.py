@@ -180,7 +180,7 @@ def _expand(transforms, N):
     return transforms
 
 
-PRECISION = {"default": 0, "native": 1, "tc": 2}
+PRECISION = {"default": 0, "native": 1, "tc": 2, "fx": 3}
 
 # FFTW planner flags (FFTW.jl values); PencilFFTs passes fftw_flags to FFTW's
 # planner, default FFTW.ESTIMATE (reference src/plans.jl:241-320)
@@ -248,9 +248,11 @@ class PencilFFTPlan:
     ``proc_dims`` must be all ones (one GPU, no MPI).  ``precision`` selects
     the kernel arithmetic: "default" (Float64 plans: double-float on the FP32
     pipes for power-of-two lines, FP64 elsewhere), "native" (Float64 plans:
-    FP64 everywhere) or "tc" (Float32 plans: c2c lines of 256, 512 and 1024
-    points as tensor-core DFT-matrix products with a tf32 hi/lo split; rel. L2
-    about 1e-6).  ``fftw_flags`` other than FFTW.ESTIMATE (e.g. FFTW.MEASURE =
+    FP64 everywhere), "fx" (Float64 plans: block floating point, 64-bit
+    integer components with one power-of-two scale per line, for
+    power-of-two lines) or "tc" (Float32 plans: c2c lines of 256, 512 and
+    1024 points as tensor-core DFT-matrix products with a tf32 hi/lo split;
+    rel. L2 about 1e-6).  ``fftw_flags`` other than FFTW.ESTIMATE (e.g. FFTW.MEASURE =
     0), or ``autotune=True``, make plan creation time the alternative kernels
     of each pass and keep the faster, as FFTW measures its candidates.
     ``fftw_timelimit`` and ``transpose_method`` are accepted and ignored, as

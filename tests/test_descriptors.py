@@ -178,6 +178,13 @@ def test_tc_split_precision_descriptor():
         P.plan_query((8, 8), T.FFT(), np.float32, precision="bf16")
 
 
+def test_block_float_precision_descriptor():
+    """The block floating point form is a Float64-only precision mode."""
+    P.plan_query((64, 512, 256), T.RFFT(), np.float64, precision="fx")
+    with pytest.raises(P.ArgumentError, match="Float64"):
+        P.plan_query((64, 512, 256), T.FFT(), np.float32, precision="fx")
+
+
 def test_fftw_flags_select_measurement():
     """FFTW.ESTIMATE (the reference's default) plans without measuring; any
     other planner flag, or autotune=True, measures."""

@@ -101,11 +101,12 @@ def test_small_and_unit_sizes(cuda, dims):
         check_plan(plan)
 
 
-@pytest.mark.parametrize("precision", ["default", "native"])
+@pytest.mark.parametrize("precision", ["default", "fx", "native"])
 @pytest.mark.parametrize("dims", [(16, 12, 6), (64, 32, 16), (8, 4096), (4096, 3), (512, 8, 2)])
 @pytest.mark.parametrize("tr", [T.RFFT(), T.FFT(), T.BFFT(), T.RFFT_(), T.FFT_()], ids=repr)
 def test_pow2_fast_path(cuda, dims, tr, precision):
-    """Power-of-two lines (register Stockham kernel), both Float64 arithmetics."""
+    """Power-of-two lines (register Stockham kernel), every Float64 arithmetic
+    (double-float, block floating point, native FP64)."""
     plan = P.PencilFFTPlan(dims, tr, F64, precision=precision)
     check_plan(plan)
     if precision == "default":
@@ -120,9 +121,10 @@ def test_fast_path_layouts(cuda, permute, edims):
                                    permute_dims=permute, extra_dims=edims))
 
 
-def test_dd_wide_dynamic_range(cuda):
+@pytest.mark.parametrize("precision", ["default", "fx"])
+def test_dd_wide_dynamic_range(cuda, precision):
     """Float64 data far outside the float exponent range keeps full accuracy."""
-    plan = P.PencilFFTPlan((64, 32, 16), T.RFFT(), F64)
+    plan = P.PencilFFTPlan((64, 32, 16), T.RFFT(), F64, precision=precision)
     orc = oracle_plan(plan)
     rng = np.random.default_rng(5)
     for scale in (1e-200, 1e250):
@@ -133,14 +135,16 @@ def test_dd_wide_dynamic_range(cuda):
         assert rel(plan.ldiv(B).to_logical(), x) <= 1e-13
 
 
+@pytest.mark.parametrize("precision", ["default", "fx"])
 @pytest.mark.parametrize("dims, tr", [((64, 32, 16), T.RFFT()), ((16, 8, 4, 6), T.FFT()),
                                       ((8, 64), (T.FFT(), T.FFT()))])
-def test_dd_line_scales(cuda, dims, tr):
-    """Float64 runs scale each first-pass line by its own largest exponent
-    and rescale in the next pass: lines whose magnitudes differ by up to
-    1e+-60 within one array, and all-zero lines, keep the 1e-13 bound
-    (forward against the oracle and round trip), in both directions."""
-    plan = P.PencilFFTPlan(dims, tr, F64)
+def test_dd_line_scales(cuda, dims, tr, precision):
+    """Float64 runs scale each line by its own largest exponent (dd: the
+    first pass's lines, rescaled to the run exponent in the next pass; fx:
+    every pass's lines): lines whose magnitudes differ by up to 1e+-60 within
+    one array, and all-zero lines, keep the 1e-13 bound (forward against the
+    oracle and round trip), in both directions."""
+    plan = P.PencilFFTPlan(dims, tr, F64, precision=precision)
     orc = oracle_plan(plan)
     rng = np.random.default_rng(11)
     x = random_input(plan, 11)
