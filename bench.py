@@ -374,8 +374,9 @@ def run_gpu(args, rank, world, local_rank):
                "pipelined": "copy-in / transforms / copy-out on three streams, double-buffered",
                "samples_ms": samples, "statistic": "median of 3 timed repetitions of the K steps"}
         # the result of the last step round-trips the input
-        err = (host_out[(args.steps - 1) & 1].double() - host_in.double()).norm() / host_in.double().norm()
-        e2e["round_trip_rel_l2"] = float(err)
+        diff = host_out[(args.steps - 1) & 1].double() - host_in.double()
+        e2e["round_trip_rel_l2"] = float(diff.norm() / host_in.double().norm())
+        e2e["round_trip_max_rel"] = float(diff.abs().max() / host_in.double().abs().max())
 
     if rank != 0:
         return
@@ -394,7 +395,13 @@ def run_gpu(args, rank, world, local_rank):
                    "l2": "inputs larger than L2 (1.07 GB arrays)",
                    "precision": args.precision,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        # per direction: the forward (mul!) and backward (ldiv!) passes' device time
+        "forward_ms": sum(e["total_ms"] for e in timing if e["direction"] > 0) / args.steps,
+        "backward_ms": sum(e["total_ms"] for e in timing if e["direction"] < 0) / args.steps,
         "hbm_gbs": alg_rt / (ms_step * 1e-3) / 1e9 * world,
+        # compulsory bytes: one read of the input and one write of the output
+        # per direction, 2 (R + C)
+        "compulsory_gbs": 2 * (R + C) / (ms_step * 1e-3) / 1e9 * world,
         "gflops": 2 * 2.5 * np.prod(dims) * np.log2(np.prod(dims)) / (ms_step * 1e-3) / 1e9 * world,
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
