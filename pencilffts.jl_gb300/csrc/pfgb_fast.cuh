@@ -685,7 +685,13 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * T)] = v[r];
   }
   __syncthreads();
-  const int nth = blockDim.x;
+  // the launch's thread count (fast_pass and fast_pass_tma launch
+  // fast_threads(LOGM, OP)); as a compile-time constant for dd, whose store
+  // loops then get constant trip counts and index steps (r2c and c2r passes
+  // of the 512^3 Float64 round trip 0.788 -> 0.778 and 0.885 -> 0.877 ms),
+  // read at run time for float, whose 32-register kernels spill with the
+  // unrolled loops (Float32 round trip 1.457 -> 1.504 ms)
+  const int nth = sizeof(R) == 4 ? (int)blockDim.x : fast_threads<R>(LOGM, OP);
   // output exponent of complex line i (the first pass of a run scales lines
   // separately; the loops below write other threads' lines)
   auto line_emax_out = [&](int i) { return IO::kDD && a.self_scale ? lexp[i] + a.emax_shift : emax_out; };
@@ -990,7 +996,7 @@ __device__ __forceinline__ void fast_tile_fx(const FastArgs& a, int64_t bid, Cx<
     if (b == 0 && p < ncl_valid)
       a.te_out[t0 / (packed ? 2 : 1) + p + a.te_ncl * div31((unsigned)bid, a.div_tiles)] = te_word(p);
   }
-  const int nth = blockDim.x;
+  constexpr int nth = fast_threads<fx>(LOGM, OP);  // the launch's thread count
   if constexpr (OP == OP_C2C) {
     const int tot = TW * M;
     for (int e = tid; e < tot; e += nth) {
