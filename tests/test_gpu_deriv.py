@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import pencilffts_gb300 as P
-from helpers import T, TOL, input_array, oracle_plan, rel
+from helpers import T, TOL, input_array, oracle_plan, random_input, rel
 from oracle import pencilfft_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -45,6 +45,31 @@ def test_fused_derivative_matches_oracle(cuda, dims, tr, real):
         P.ldiv_(U, plan, S, deriv=(d + 1, L[d]))
         assert np.array_equal(S.to_logical(), before)  # the spectrum is not modified
         assert rel(U.to_logical(), orc.ldiv(ik * spec)) <= TOL[np.dtype(real)]
+
+
+@pytest.mark.parametrize("dims,tr", [((64, 32, 48), T.RFFT()), ((32, 24, 40), T.FFT())],
+                         ids=["rfft", "fft-mixed"])
+def test_fused_derivative_block_float_plan(cuda, dims, tr):
+    """A Float64 plan in block floating point (precision="fx") runs a fused
+    derivative with its double-float kernels; plain executions of the same
+    plan before and after stay in fx, match the oracle and repeat bit for
+    bit."""
+    plan = P.PencilFFTPlan(dims, tr, np.float64, precision="fx")
+    orc = oracle_plan(plan)
+    x = random_input(plan, 13)
+    A = input_array(plan, x)
+    spec = orc.forward(x)
+    B0 = plan * A
+    assert rel(B0.to_logical(), spec) <= 1e-13
+    L = (2 * np.pi, 3.0)
+    B = plan.allocate_output()
+    P.mul_(B, plan, A, deriv=(1, L[0]))
+    assert rel(B.to_logical(), O.wavenumbers(orc, 0, L[0]) * spec) <= 1e-13
+    U = plan.allocate_input()
+    P.ldiv_(U, plan, B0, deriv=(2, L[1]))
+    assert rel(U.to_logical(), orc.ldiv(O.wavenumbers(orc, 1, L[1]) * spec)) <= 1e-13
+    assert np.array_equal((plan * A).to_logical(), B0.to_logical())
+    assert rel(plan.ldiv(B0).to_logical(), x) <= 1e-13
 
 
 def test_taylor_green_vorticity_fused(cuda):
