@@ -4,9 +4,9 @@
 `ccall` binding of libpencilfft_gb300 (C ABI in include/pencilfft_gb300.h) for
 PencilFFTs.jl at `proc_dims = (1, ..., 1)` on one GB300 GPU.
 
-`GB300Plan(dims, transforms, real_type; permute_dims, extra_dims)` is the device
-counterpart of `PencilFFTPlan(dims, transforms, proc_dims, comm, real_type; ...)`
-(reference src/plans.jl:306-320); `mul!`, `ldiv!` and `bmul!` take `CuArray`s
+`GB300Plan(dims, transforms, real_type; permute_dims, extra_dims, fftw_flags,
+precision)` is the device counterpart of `PencilFFTPlan(dims, transforms,
+proc_dims, comm, real_type; ...)` (reference src/plans.jl:306-320); `mul!`, `ldiv!` and `bmul!` take `CuArray`s
 laid out as the reference's `PencilArray` parents: input in natural order,
 output with its dimensions reversed when `permute_dims = Val(true)`.
 
@@ -42,6 +42,14 @@ struct PlanDesc
     autotune::Int32
 end
 
+# PFGB_PRECISION_* (include/pencilfft_gb300.h): :default (Float64 power-of-two
+# lines in double-float), :native (FP64 everywhere), :tc (Float32 tensor-core
+# split form), :fx (Float64 block floating point)
+const PRECISION = Dict(:default => Int32(0), :native => Int32(1), :tc => Int32(2), :fx => Int32(3))
+
+# planner measurement, as FFTW measures its candidates for any flag but ESTIMATE
+autotune_code(flags) = Int32(flags & FFTW.ESTIMATE == 0)
+
 abi_kind(::Union{Transforms.FFT,Transforms.FFT!}) = Int32(0)
 abi_kind(::Union{Transforms.BFFT,Transforms.BFFT!}) = Int32(1)
 abi_kind(::Union{Transforms.RFFT,Transforms.RFFT!}) = Int32(2)
@@ -70,7 +78,10 @@ mutable struct GB300Plan{T,N}
     transforms::NTuple{N,Transforms.AbstractTransform}
     scale::Float64
     function GB300Plan(dims::Dims{N}, transforms, ::Type{T} = Float64;
-                       permute_dims::Val{P} = Val(true), extra_dims::Dims = ()) where {N,T,P}
+                       permute_dims::Val{P} = Val(true), extra_dims::Dims = (),
+                       fftw_flags = FFTW.ESTIMATE, precision::Symbol = :default) where {N,T,P}
+        haskey(PRECISION, precision) ||
+            throw(ArgumentError("precision must be one of $(Tuple(keys(PRECISION)))"))
         trs = transforms isa Transforms.AbstractTransform ?
               Transforms.expand_dims(transforms, Val(N)) : transforms
         desc = PlanDesc(Int32(N), pad(Int64.(dims), MAX_DIMS, 0),
@@ -79,7 +90,8 @@ mutable struct GB300Plan{T,N}
                         pad(map(r2r_code, trs), MAX_DIMS, Int32(0)),
                         pad(map(even_code, trs), MAX_DIMS, Int32(0)),
                         Int32(sizeof(T)), Int32(P), Int32(length(extra_dims)),
-                        pad(Int64.(extra_dims), MAX_EXTRA, 0), Int32(0), Int32(0))
+                        pad(Int64.(extra_dims), MAX_EXTRA, 0), PRECISION[precision],
+                        autotune_code(fftw_flags))
         h = Ref{Ptr{Cvoid}}(C_NULL)
         check(ccall((:pfgb_plan_create, LIB), Cint, (Ref{PlanDesc}, Ref{Ptr{Cvoid}}), desc, h))
         info = Vector{UInt8}(undef, 512)
