@@ -18,6 +18,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -120,7 +121,10 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples (the JSON line carries their summary); PFGB_CLOCKS_DIR
+        # keeps them in a chosen folder
+        self.path = os.path.join(os.environ.get("PFGB_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"clocks_bench_{os.getpid()}.csv")
 
     def start(self):
         try:

@@ -94,7 +94,7 @@ typedef struct pfgb_plan_desc {
  *             as two DFT-matrix products on the tensor cores (tf32 hi/lo
  *             split, three products, FP32 accumulation); other lines as in
  *             DEFAULT.  Relative L2 error about 1e-6 for a 3D round trip.
- *             The benchmark spec's precision form; FFTW has no such mode.
+ *             FFTW has no such mode.
  *   BLOCK_FLOAT: Float64 plans only: power-of-two c2c/r2c/c2r lines in block
  *             floating point (64-bit integer components, one power-of-two
  *             scale per line, 50 bits below each line's largest component
