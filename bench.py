@@ -22,6 +22,8 @@ import tempfile
 import sys
 import time
 
+import numpy as np
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 for _p in (REPO, os.path.join(REPO, "pencilffts.jl_gb300")):
     if _p not in sys.path:
@@ -46,6 +48,10 @@ def parse():
                     help="skip the Float32 plain vs tensor-core split comparison")
     ap.add_argument("--cpu-sample-s", type=float, default=20.0,
                     help="approximate CPU seconds for the cpu_baseline sample")
+    ap.add_argument("--configs", default="all",
+                    help="other benchmark configurations to measure after the headline: "
+                         "'all', 'none' or a comma list of C1,C2a,C2b,C3,C4,C5")
+    ap.add_argument("--config-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -53,6 +59,30 @@ def workload(args):
     dims = tuple(int(x) for x in args.dims.split(","))
     rb = 8 if args.real == "f64" else 4
     return dims, rb
+
+
+ARITHMETIC = {
+    ("f64", "default"): "dd (2xFP32, 48-bit significand) for power-of-two lines",
+    ("f64", "native"): "FP64",
+    ("f64", "fx"): "block floating point (int64 components, per-line exponent)",
+    ("f32", "default"): "FP32",
+    ("f32", "tc"): "FP32 with 3xTF32 tensor-core DFT products for 256/512/1024-point c2c lines",
+}
+
+
+def headline_config(args, world):
+    """The workload description both arms print (identical dicts)."""
+    dims, rb = workload(args)
+    arith = ARITHMETIC.get((args.real, args.precision), args.precision)
+    return {"workload": f"RFFT round trip {'x'.join(map(str, dims))} "
+                        f"{'Float64' if rb == 8 else 'Float32'} (mul! + ldiv!), "
+                        "permute_dims=true, out-of-place",
+            "dims": list(dims), "transforms": "RFFT (RFFT, FFT, FFT)",
+            "l2": (f"inputs larger than L2 ({int(np.prod(dims)) * rb / 1e9:.2f} GB arrays)"
+                   if int(np.prod(dims)) * rb > 129e6 else "inputs L2-resident (smaller than 129 MB)"),
+            "precision": f"{'Float64' if rb == 8 else 'Float32'} data; GB300 arm: {arith}; "
+                         "reference arm: FP64 (oracle, scipy.fft)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
 def alg_bytes_round_trip(dims, rb):
@@ -225,6 +255,358 @@ def measure_forms(P, dims, steps, warmup, dev):
 
 
 # ---------------------------------------------------------------------------
+# The other benchmark configurations (C1-C5).  Each is timed on the device as
+# mul! + ldiv! per step (the reference benchmark loop), with the dominant
+# kernel's roofline from per-pass events; its CPU leg times the oracle on the
+# same input and, as the checker, gives the forward rel. L2 of the GPU output
+# against it.
+# ---------------------------------------------------------------------------
+def _rel(a, b, chunk=1 << 24):
+    """|a - b| / |b| in float64 over chunks (host arrays)."""
+    import numpy as np
+    a = np.asarray(a).reshape(-1)
+    b = np.asarray(b).reshape(-1)
+    num = den = 0.0
+    for i in range(0, a.size, chunk):
+        x, y = a[i:i + chunk], b[i:i + chunk]
+        num += float(np.sum(np.abs(x.astype(np.complex128) - y) ** 2))
+        den += float(np.sum(np.abs(y) ** 2))
+    return (num / den) ** 0.5 if den > 0 else num ** 0.5
+
+
+def _rel_dev(a, b):
+    """|a - b| / |b| on the device, in float64."""
+    import torch
+    a = torch.view_as_real(a) if a.is_complex() else a
+    b = torch.view_as_real(b) if b.is_complex() else b
+    return (torch.linalg.vector_norm((a.double() - b.double()).reshape(-1)) /
+            torch.linalg.vector_norm(b.double().reshape(-1))).item()
+
+
+def _peak():
+    try:
+        return float(json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _roofline(timing, steps):
+    """Dominant kernel (largest summed event time) of the per-pass records of
+    `steps` timed steps: algorithmic bytes per launch / average duration."""
+    per = {}
+    for e in timing:
+        k = per.setdefault(e["kernel"], {"ms": 0.0, "bytes": 0, "launches": 0})
+        k["ms"] += e["total_ms"]
+        k["bytes"] += e["bytes_per_launch"] * e["launches"]
+        k["launches"] += e["launches"]
+    name, d = max(per.items(), key=lambda kv: kv[1]["ms"])
+    peak, src = _peak()
+    bpl = d["bytes"] / d["launches"]
+    avg_s = d["ms"] / d["launches"] * 1e-3
+    ach = bpl / avg_s / 1e9
+    return {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "peak_source": src,
+            "unit": "GB/s", "frac": ach / peak, "alg_bytes_per_launch": bpl,
+            "avg_launch_ms": avg_s * 1e3, "launches_per_step": sum(v["launches"] for v in per.values()) / steps,
+            "kernel_share": d["ms"] / sum(v["ms"] for v in per.values())}
+
+
+def _timed(steps, warmup, step, plans=()):
+    """ms per step (CUDA events on the current stream, synchronised on both
+    sides) and the plans' per-pass records of the timed steps."""
+    import torch
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    for p in plans:
+        p.set_timing(True)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    timing = []
+    for p in plans:
+        timing += p.get_timing()
+        p.set_timing(False)
+    return e0.elapsed_time(e1) / steps, timing
+
+
+def _oracle_leg(forward, x, got):
+    """cpu_baseline leg of a configuration: the oracle's forward transform of
+    the same input, timed on the host threads, and (as the checker) the rel.
+    L2 of the GPU forward output against it."""
+    t0 = time.perf_counter()
+    ref = forward(x)
+    ms = (time.perf_counter() - t0) * 1e3
+    return ms, _rel(got, ref)
+
+
+def _round_trip_config(P, O, steps, warmup, dims, transforms, real, x, workload, data, gflop=None):
+    import numpy as np
+    import torch
+    plan = P.PencilFFTPlan(dims, transforms, real)
+    u, v, w = plan.allocate_input(), plan.allocate_output(), plan.allocate_input()
+    u.copy_from_logical(x)
+
+    def step():
+        P.mul_(v, plan, u)
+        P.ldiv_(w, plan, v)
+
+    ms, timing = _timed(steps, warmup, step, (plan,))
+    alg = sum(e["bytes_per_launch"] * e["launches"] for e in timing) / steps
+    P.mul_(v, plan, u)
+    P.ldiv_(w, plan, v)
+    got, back = v.to_logical(), w.to_logical()
+    orc = O.OraclePlan(dims, tuple(_to_oracle(O, P, t) for t in plan.transforms), np.dtype(real))
+    threads = os.cpu_count() or 1
+    import scipy.fft as sfft
+    with sfft.set_workers(threads):
+        fwd_ms, err = _oracle_leg(orc.forward, x, got)
+    out = {"workload": workload, "data": data, "dims": list(dims),
+           "value": ms, "unit": "ms", "metric": "round trip (mul! + ldiv!) ms",
+           "forward_ms": sum(e["total_ms"] for e in timing if e["direction"] > 0) / steps,
+           "backward_ms": sum(e["total_ms"] for e in timing if e["direction"] < 0) / steps,
+           "alg_bytes_per_round_trip": alg, "hbm_gbs": alg / (ms * 1e-3) / 1e9,
+           "roofline": _roofline(timing, steps),
+           "rel_l2_forward_vs_oracle": err, "rel_l2_round_trip": _rel(back, x),
+           "cpu_baseline": {"value": fwd_ms, "unit": "ms per forward", "cores": threads, "kind": "port",
+                            "sample": "one forward transform of the same input (oracle, scipy.fft)"}}
+    if gflop is not None:
+        out["gflops"] = gflop / (ms * 1e-3)
+    del plan, u, v, w
+    torch.cuda.empty_cache()
+    return out
+
+
+def _to_oracle(O, P, tr):
+    T = P.Transforms
+    if isinstance(tr, T.FFT):
+        return O.Tr("FFT", tr.inplace)
+    if isinstance(tr, T.BFFT):
+        return O.Tr("BFFT", tr.inplace)
+    if isinstance(tr, T.RFFT):
+        return O.Tr("RFFT", tr.inplace)
+    if isinstance(tr, T.BRFFT):
+        return O.Tr("BRFFT", tr.inplace, even=tr.even_output)
+    if isinstance(tr, T.R2R):
+        return O.Tr("R2R", tr.inplace, kind=tr.kind)
+    return O.Tr("NoTransform", tr.inplace)
+
+
+def _flop_c2c(n):
+    import numpy as np
+    return 2 * 5 * n * np.log2(n) / 1e9  # forward + backward, 5 N log2 N each
+
+
+def _flop_r2c(n):
+    import numpy as np
+    return 2 * 2.5 * n * np.log2(n) / 1e9
+
+
+def config_c1(P, O, steps, warmup):
+    import numpy as np
+    dims = (16, 32, 64)
+    x = np.random.default_rng(42).random(dims)
+    return _round_trip_config(P, O, steps, warmup, dims, P.Transforms.RFFT(), np.float64, x,
+                              "RFFT round trip 16x32x64 Float64", "uniform [0,1), seed 42 (L2-resident)",
+                              _flop_r2c(np.prod(dims)))
+
+
+def config_c2a(P, O, steps, warmup):
+    import numpy as np
+    dims = (256, 256, 256)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(dims) + 1j * rng.standard_normal(dims)
+    return _round_trip_config(P, O, steps, warmup, dims, P.Transforms.FFT(), np.float64, x,
+                              "FFT + BFFT (ldiv!) round trip 256^3 ComplexF64",
+                              "N(0,1) real and imaginary parts, seed 0 (268 MB arrays)",
+                              _flop_c2c(np.prod(dims)))
+
+
+def config_c2b(P, O, steps, warmup):
+    import numpy as np
+    dims = (512, 512, 512)
+    x = np.random.default_rng(1).uniform(-1, 1, dims).astype(np.float32)
+    return _round_trip_config(P, O, steps, warmup, dims, P.Transforms.RFFT(), np.float32, x,
+                              "RFFT round trip 512^3 Float32", "uniform [-1,1), seed 1 (537 MB arrays)",
+                              _flop_r2c(np.prod(dims)))
+
+
+def config_c3(P, O, steps, warmup):
+    import numpy as np
+    T = P.Transforms
+    nx, ny, nz = 512, 512, 257
+    xs = 2 * np.pi * np.arange(nx) / nx
+    ys = 2 * np.pi * np.arange(ny) / ny
+    zs = np.cos(np.pi * np.arange(nz) / (nz - 1))
+    u = np.sin(xs)[:, None, None] * np.cos(ys)[None, :, None] * np.cos(zs)[None, None, :]
+    return _round_trip_config(P, O, steps, warmup, (nx, ny, nz), (T.RFFT(), T.FFT(), T.R2R(T.REDFT00)),
+                              np.float64, u,
+                              "(RFFT, FFT, R2R{REDFT00}) round trip 512x512x257 Float64",
+                              "Taylor-Green sin x cos y cos z, Chebyshev-Gauss-Lobatto z (539 MB arrays)",
+                              _flop_r2c(512 ** 3))
+
+
+def config_c4(P, O, steps, warmup):
+    """1024^3 Float32 RFFT, plain and tensor-core split form; errors against
+    the Float64 plan on the same input (the double-float path, itself
+    parity-tested against the FP64 oracle at 1e-13; a 1024^3 CPU oracle per
+    run is too slow)."""
+    import numpy as np
+    import torch
+    n = 1024
+    dims = (n, n, n)
+    T = P.Transforms
+    rng = np.random.default_rng(1234)
+    amps, phis, ks = rng.uniform(1, 10, 8), rng.uniform(0, 2 * np.pi, 8), rng.integers(0, 64, size=(8, 3))
+    p64 = P.PencilFFTPlan(dims, T.RFFT(), np.float64)
+    u64 = p64.allocate_input()
+    g = torch.Generator(device="cuda").manual_seed(1234)
+    u64.data.normal_(generator=g)
+    lin = torch.arange(n, device="cuda", dtype=torch.float64) * (2 * np.pi / n)
+    for a, phi, k in zip(amps, phis, ks):
+        ph = (k[2] * lin)[:, None, None] + (k[1] * lin)[None, :, None] + (k[0] * lin)[None, None, :]
+        u64.data.add_(a * torch.cos(ph + phi))
+        del ph
+    u64.data.copy_(u64.data.float().double())  # the Float32 input, exactly
+    ref = p64 * u64
+    del p64
+    torch.cuda.empty_cache()
+    out = {"workload": "RFFT round trip 1024^3 Float32, plain and tensor-core split forms",
+           "data": "N(0,1) + 8 random-amplitude Fourier modes, seed 1234 (4.3 GB arrays)", "dims": list(dims)}
+    for name, prec in (("f32_plain", "default"), ("f32_tc_split", "tc")):
+        p = P.PencilFFTPlan(dims, T.RFFT(), np.float32, precision=prec)
+        u, v, w = p.allocate_input(), p.allocate_output(), p.allocate_input()
+        u.data.copy_(u64.data)
+
+        def step():
+            P.mul_(v, p, u)
+            P.ldiv_(w, p, v)
+
+        ms, timing = _timed(steps, warmup, step, (p,))
+        alg = sum(e["bytes_per_launch"] * e["launches"] for e in timing) / steps
+        P.mul_(v, p, u)
+        P.ldiv_(w, p, v)
+        out[name] = {"value": ms, "unit": "ms", "hbm_gbs": alg / (ms * 1e-3) / 1e9,
+                     "gflops": _flop_r2c(n ** 3) / (ms * 1e-3), "roofline": _roofline(timing, steps),
+                     "rel_l2_forward_vs_f64": _rel_dev(v.data, ref.data),
+                     "rel_l2_round_trip": _rel_dev(w.data, u.data),
+                     "device_status": p.device_status()}
+        del p, u, v, w
+        torch.cuda.empty_cache()
+    out["tc_split_speedup_vs_plain"] = out["f32_plain"]["value"] / out["f32_tc_split"]["value"]
+    del u64, ref
+    torch.cuda.empty_cache()
+    return out
+
+
+def config_c5(P, O, steps, warmup):
+    """(i) 3 x 384^3 Float32: per component c, r2c, i k_c multiply fused into
+    the first backward pass, c2r (the derivative along dimension c);
+    (ii) 64 independent r2c/c2r round trips of sizes drawn from 48..192 per
+    axis, recorded once into a CUDA graph (Batch) and replayed."""
+    import numpy as np
+    import scipy.fft as sfft
+    import torch
+    T = P.Transforms
+    threads = os.cpu_count() or 1
+    out = {}
+    # (i) vector field
+    n = 384
+    dims = (n, n, n)
+    plan = P.PencilFFTPlan(dims, T.RFFT(), np.float32)
+    rng = np.random.default_rng(2024)
+    comps = [rng.standard_normal(dims).astype(np.float32) for _ in range(3)]
+    us = plan.allocate_input(P.Val(3))
+    vs = plan.allocate_output(P.Val(3))
+    ds = plan.allocate_input(P.Val(3))
+    for c, x in zip(us, comps):
+        c.copy_from_logical(x)
+    L = 2 * np.pi
+
+    def step():
+        for c in range(3):
+            P.mul_(vs[c], plan, us[c])
+            P.ldiv_(ds[c], plan, vs[c], deriv=(c + 1, L))
+
+    ms, timing = _timed(steps, warmup, step, (plan,))
+    alg = sum(e["bytes_per_launch"] * e["launches"] for e in timing) / steps
+    step()
+    orc = O.OraclePlan(dims, O.RFFT(), np.float32)
+    errs = []
+    t0 = time.perf_counter()
+    with sfft.set_workers(threads):
+        for c in range(3):
+            ref = orc.ldiv(orc.forward(comps[c]) * O.wavenumbers(orc, c, L))
+            errs.append(_rel(ds[c].to_logical(), ref))
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    out["vector_gradient_384"] = {
+        "workload": "3 x 384^3 Float32: r2c, i k_c fused into the first backward pass, c2r (per component)",
+        "data": "N(0,1), seed 2024 (227 MB per component)", "value": ms, "unit": "ms per 3 components",
+        "hbm_gbs": alg / (ms * 1e-3) / 1e9, "roofline": _roofline(timing, steps),
+        "rel_l2_vs_oracle_max": max(errs),
+        "cpu_baseline": {"value": cpu_ms, "unit": "ms per 3 components", "cores": threads, "kind": "port",
+                         "sample": "oracle forward, i k multiply and ldiv of the 3 components"}}
+    del plan, us, vs, ds
+    torch.cuda.empty_cache()
+    # (ii) 64 uneven fields
+    rng = np.random.default_rng(2024)
+    sizes = [tuple(int(s) for s in rng.integers(48, 193, 3)) for _ in range(64)]
+    plans, arrs, xs = [], [], []
+    for d in sizes:
+        p = P.PencilFFTPlan(d, T.RFFT(), np.float32)
+        u, v, w = p.allocate_input(), p.allocate_output(), p.allocate_input()
+        x = rng.standard_normal(d).astype(np.float32)
+        u.copy_from_logical(x)
+        plans.append(p)
+        arrs.append((u, v, w))
+        xs.append(x)
+    alg = 0
+    for p, (u, v, w) in zip(plans, arrs):
+        _, t = _timed(1, 0, lambda: (P.mul_(v, p, u), P.ldiv_(w, p, v)), (p,))
+        alg += sum(e["bytes_per_launch"] * e["launches"] for e in t)
+
+    def seq():
+        for p, (u, v, w) in zip(plans, arrs):
+            P.mul_(v, p, u)
+            P.ldiv_(w, p, v)
+
+    ms_seq, _ = _timed(steps, warmup, seq)
+    ops = []
+    for p, (u, v, w) in zip(plans, arrs):
+        ops += [(P.mul_, v, p, u), (P.ldiv_, w, p, v)]
+    batch = P.Batch(ops)
+    ms_graph, _ = _timed(steps, warmup, batch.launch)
+    batch.launch()
+    torch.cuda.synchronize()
+    errs, rts = [], []
+    t0 = time.perf_counter()
+    for p, (u, v, w), x, d in zip(plans, arrs, xs, sizes):
+        o = O.OraclePlan(d, O.RFFT(), np.float32)
+        errs.append(_rel(v.to_logical(), o.forward(x)))
+        rts.append(_rel(w.to_logical(), x))
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    out["uneven_64"] = {
+        "workload": "64 independent r2c + c2r round trips, sizes ~U{48..192} per axis (seed 2024)",
+        "data": "N(0,1) (fields of 0.4-28 MB, L2-resident)", "value": ms_graph, "unit": "ms per 64 round trips",
+        "sequential_ms": ms_seq, "graph_speedup_vs_sequential": ms_seq / ms_graph,
+        "hbm_gbs": alg / (ms_graph * 1e-3) / 1e9, "alg_bytes": alg,
+        "rel_l2_forward_vs_oracle_max": max(errs), "rel_l2_round_trip_max": max(rts),
+        "cpu_baseline": {"value": cpu_ms, "unit": "ms (oracle forwards of the 64 fields, checker included)",
+                         "cores": 1, "kind": "port", "sample": "one forward per field"}}
+    del batch, plans, arrs
+    torch.cuda.empty_cache()
+    return out
+
+
+CONFIGS = {"C1": config_c1, "C2a": config_c2a, "C2b": config_c2b, "C3": config_c3,
+           "C4": config_c4, "C5": config_c5}
+
+
+# ---------------------------------------------------------------------------
 # the GB300 arm
 # ---------------------------------------------------------------------------
 def run_gpu(args, rank, world, local_rank):
@@ -245,7 +627,9 @@ def run_gpu(args, rank, world, local_rank):
         cpu_baseline = {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
                         "sample": f"{iters} full {'x'.join(map(str, dims))} "
                                   f"{'Float64' if rb == 8 else 'Float32'} RFFT round trips "
-                                  f"(oracle: scipy.fft pocketfft, {threads} threads)"}
+                                  f"(oracle: scipy.fft pocketfft, {threads} threads; Julia and "
+                                  "FFTW are not installed, so the reference's FFTW path is "
+                                  "replaced by this restatement)"}
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -384,21 +768,50 @@ def run_gpu(args, rank, world, local_rank):
 
     if rank != 0:
         return
+    # cpu_baseline leg, as the checker: the GPU forward and ldiv! of the
+    # benchmark's input against the oracle (scipy.fft, FP64, host threads)
+    parity = None
+    if not args.no_cpu_baseline:
+        import scipy.fft as sfft
+        from oracle import pencilfft_oracle as O
+        x = u.to_logical()
+        P.mul_(v, plan, u)
+        got = v.to_logical()
+        back = plan.ldiv(v).to_logical()
+        orc = O.OraclePlan(dims, O.RFFT(), real)
+        with sfft.set_workers(os.cpu_count() or 1):
+            ref = orc.forward(x)
+            e_fwd = _rel(got, ref)
+            del ref
+            e_bwd = _rel(back, orc.ldiv(got))
+        parity = {"rel_l2_forward_vs_oracle": e_fwd, "rel_l2_backward_vs_oracle": e_bwd,
+                  "rel_l2_round_trip": _rel(back, x),
+                  "tolerance": 1e-13 if rb == 8 else 2e-6,
+                  "oracle": "FP64 restatement of the reference path (scipy.fft), same input"}
+        del x, got, back
     forms = None
     if not args.no_forms:
         forms = measure_forms(P, dims, args.steps, args.warmup, dev)
+    del plan, u, v
+    torch.cuda.empty_cache()
+    configs = None
+    if args.configs != "none":
+        from oracle import pencilfft_oracle as O
+        names = list(CONFIGS) if args.configs == "all" else args.configs.split(",")
+        configs = {}
+        for nm in names:
+            try:
+                configs[nm] = CONFIGS[nm](P, O, args.config_steps, 3)
+            except Exception as e:  # a failing configuration is reported, not hidden
+                configs[nm] = {"error": f"{type(e).__name__}: {e}"[:500]}
+            torch.cuda.empty_cache()
     line = {
         "metric": METRIC, "value": ms_step, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if rb == 8 else "f32", "data": "synthetic: uniform [-1,1), seeded",
-        "config": {"workload": f"RFFT round trip {'x'.join(map(str, dims))} "
-                               f"{'Float64' if rb == 8 else 'Float32'} (mul! + ldiv!), "
-                               "permute_dims=true, out-of-place",
-                   "dims": list(dims), "transforms": "RFFT (RFFT, FFT, FFT)",
-                   "l2": "inputs larger than L2 (1.07 GB arrays)",
-                   "precision": args.precision,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": headline_config(args, world),
+        "arithmetic": ARITHMETIC.get((args.real, args.precision), args.precision),
         # per direction: the forward (mul!) and backward (ldiv!) passes' device time
         "forward_ms": sum(e["total_ms"] for e in timing if e["direction"] > 0) / args.steps,
         "backward_ms": sum(e["total_ms"] for e in timing if e["direction"] < 0) / args.steps,
@@ -418,7 +831,10 @@ def run_gpu(args, rank, world, local_rank):
         "gpu_launches": launches,
         "forms": forms,
         "clocks": clocks,
+        "configs": configs,
     }
+    if parity:
+        line.update(parity)
     print(json.dumps(line), flush=True)
 
 
@@ -435,9 +851,7 @@ def run_reference(args, rank, world):
         "steps": iters, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if rb == 8 else "f32",
         "data": "synthetic: uniform [-1,1), seeded",
-        "config": {"workload": f"RFFT round trip {'x'.join(map(str, dims))} "
-                               f"{'Float64' if rb == 8 else 'Float32'} (mul! + ldiv!), "
-                               "permute_dims=true, out-of-place", "dims": list(dims)},
+        "config": headline_config(args, world),
         "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{iters} full round trips (oracle: scipy.fft pocketfft, "
                                    f"{threads} threads; Julia/FFTW are not installed)"},

@@ -228,9 +228,13 @@ int pfgb_plan_get_timing(pfgb_plan* plan, pfgb_pass_timing* out, int max, int* n
  * in double-float like the Float64 plans.  Its only scratch is a fixed
  * 130,816-byte static device array (exponent word + twiddle tables), so n
  * must be a power of two in [32, 4096]; other sizes return PFGB_ERR_ARGUMENT.
- * The first call on a device (with it current) resolves the array's address
- * and fills the tables with a synchronous copy: make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * Each line is scaled by its own largest exponent, so lines of very
+ * different magnitude in one batch keep their accuracy.  The first call on a
+ * device (with it current) resolves the array's address and fills the tables
+ * with a synchronous copy: make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race.  A device reset
+ * (cudaDeviceReset) is not supported: the per-device set-up is kept for the
+ * life of the process. */
 int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* out, const void* in,
                        void* stream);
 
@@ -238,9 +242,21 @@ int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* out, const vo
  * then returns in *flags, and clears, the bits set by bounded device waits
  * that gave up since the last call (1: a TMA tile copy of fast_pass_tma,
  * 2: a tensor-core product of tc_pass; the kernel then skipped the rest of
- * its tiles).  No counterpart in the reference: FFTW calls cannot stall on
- * a device. */
+ * its tiles after waiting, again bounded, for the copies and products it had
+ * issued; 4: one of those waits gave up too, so the kernel may have released
+ * shared or tensor memory that a copy or product still wrote).  The output
+ * of an execution that set a bit is incomplete.  No counterpart in the
+ * reference: FFTW calls cannot stall on a device. */
 int pfgb_device_status(pfgb_plan* plan, void* stream, int32_t* flags);
+
+/* Test hook for the give-up path of those waits; no counterpart in the
+ * reference.  polls > 0: in later executions, the first data wait of every
+ * CTA of fast_pass_tma and tc_pass polls, `polls` times, an mbarrier that
+ * nothing signals, so it gives up and the kernel takes its failure path
+ * (status bit 1 or 2) without any wait that could hang.  tma != 0 also runs
+ * eligible c2r passes in the TMA-fed form.  polls = 0, tma = 0 restore
+ * normal execution. */
+int pfgb_plan_set_wait_test(pfgb_plan* plan, int polls, int tma);
 
 /* Copies the message of the last failure on this thread into buf. Returns the
  * message length. */

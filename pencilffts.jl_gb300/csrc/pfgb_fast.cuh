@@ -41,9 +41,7 @@ struct FastArgs {
   float scale_h, scale_l;  // ldiv! normalisation as hi + lo
   // Float64 (dd) passes: the input / output of a pass between two dd passes is
   // kept in dd form (re.hi, re.lo, im.hi, im.lo floats), scaled by the power
-  // of two 2^(1023 - *emax), *emax the run exponent (see self_scale below;
-  // callers that set neither self_scale nor te_rescale, the allocation-free
-  // entry point, compute it with emax_kernel before the pass).
+  // of two 2^(1023 - *emax), *emax the run exponent (see self_scale below).
   int in_dd, out_dd;
   const int* emax_ptr;
   // added to the run exponent for the double outputs of the pass: the ldiv!
@@ -82,6 +80,10 @@ struct FastArgs {
   // word set when a bounded wait gives up
   int64_t total;
   int* err;
+  // test of the give-up path (pfgb_plan_set_wait_test): > 0 makes the first
+  // data wait of every CTA poll, this many times, an mbarrier that nothing
+  // signals, so that it gives up
+  int wait_test;
   // tensor-core split form: the DFT matrices' tf32 hi / lo parts in the
   // shared-memory operand layout (tc_pass)
   const void* tcb;
@@ -1119,8 +1121,11 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-  for (int i = 0; i < (1 << 22); ++i)
+// polls of a bounded wait before it gives up
+constexpr int kWaitPolls = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  int polls = kWaitPolls) {
+  for (int i = 0; i < polls; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -1173,7 +1178,9 @@ __host__ __device__ constexpr int tma_min_blocks(int logm) {
 template <typename R, int LOGM, int SIGN, int IOM>
 __global__ void __launch_bounds__(fast_threads<R>(LOGM, OP_C2R), tma_min_blocks<R>(LOGM)) fast_pass_tma(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long bars[2];
+  // bars[0..1]: the two tile buffers' copies; bars[2]: never signalled (the
+  // give-up test's wait)
+  __shared__ __align__(8) unsigned long long bars[3];
   __shared__ int s_fail;
   Cx<R>* z = reinterpret_cast<Cx<R>*>(smem_raw);
   const size_t zb = (fast_smem<R>(LOGM, OP_C2R) + 127) / 128 * 128;
@@ -1183,6 +1190,7 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM, OP_C2R), tma_min_blocks<
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_fail = 0;
   }
@@ -1194,7 +1202,9 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM, OP_C2R), tma_min_blocks<
     const int64_t nxt = tile + gridDim.x;
     if (threadIdx.x == 0 && nxt < a.total)
       tma_issue<R, LOGM>(a, nxt, buf0 + ((it + 1) & 1) * tb, &bars[(it + 1) & 1]);
-    if (!mbar_wait_bounded(&bars[it & 1], (it >> 1) & 1)) s_fail = 1;
+    const bool ok = a.wait_test > 0 ? mbar_wait_bounded(&bars[2], 0, a.wait_test)
+                                    : mbar_wait_bounded(&bars[it & 1], (it >> 1) & 1);
+    if (!ok) s_fail = 1;
     __syncthreads();
     if (s_fail) break;
     fast_tile<R, LOGM, SIGN, OP_C2R, IOM>(a, tile, z, buf0 + (it & 1) * tb, 0, 1, line_elems);
@@ -1202,10 +1212,13 @@ __global__ void __launch_bounds__(fast_threads<R>(LOGM, OP_C2R), tma_min_blocks<
   }
   if (s_fail && threadIdx.x == 0) {
     atomicOr(a.err, 1);
-    // the copy issued for the next tile may still be in flight: wait for it
-    // (bounded) before the CTA's shared memory is released
+    // the copies this CTA issued may still be in flight (the tile whose wait
+    // gave up, and the next tile): wait for both, bounded, before the CTA's
+    // shared memory is released; bit 4 if one of them does not complete
+    bool drained = mbar_wait_bounded(&bars[it & 1], (it >> 1) & 1);
     const int64_t nxt = tile + gridDim.x;
-    if (nxt < a.total) mbar_wait_bounded(&bars[(it + 1) & 1], ((it + 1) >> 1) & 1);
+    if (nxt < a.total) drained = mbar_wait_bounded(&bars[(it + 1) & 1], ((it + 1) >> 1) & 1) && drained;
+    if (!drained) atomicOr(a.err, 4);
   }
 }
 

@@ -12,21 +12,26 @@
 // arrays, and the only other device memory the kernels touch is the
 // file-scope array below.
 //
-// Scratch: g_noalloc_scratch holds the exponent word of the double-float
-// scale (written by emax_kernel, read by fast_pass<dd>) and the double-float
+// Scratch: g_noalloc_scratch holds an exponent word and the double-float
 // twiddle tables of every power-of-two length 32..4096 (8160 entries of 16
 // bytes).  It is 130,816 bytes, resident on every GPU that loads the library
-// until the process exits.  Every call shares it and it keeps the last call's
-// contents: the exponent word is cleared by each call before use and the
-// tables are written once per device and then only read, so calls that
-// overlap on the GPU (different streams, or different host threads) race on
-// the exponent word and must be serialised by the caller.
+// until the process exits.  Each line is scaled by its own largest exponent
+// (the kernel's per-line scaling), so lines of very different magnitude in
+// one batch keep their full accuracy; the exponent word only collects the
+// lines' exponents (atomicMax) and no result depends on it.  Every call
+// shares the array and it keeps the last call's contents: the tables are
+// written once per device and then only read, and the word is never cleared.
+// Calls that overlap on the GPU (different streams, or different host
+// threads) write the word concurrently; that race changes no result, but the
+// library makes no other promise for overlapping calls: serialise them.
 //
 // Set-up: the first call on a device (with that device current) resolves the
 // device address of the array with cudaGetSymbolAddress and fills the tables
 // with cudaMemcpyToSymbol, which is a synchronous host-to-device copy; make
 // that first call before any stream capture.  Later calls on the same device
-// only launch kernels.
+// only launch kernels.  The set-up is cached per device index for the life of
+// the process: a device reset (cudaDeviceReset) is not supported, since the
+// cached address and tables would belong to the released context.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -44,7 +49,6 @@ namespace pfgb {
 int fail_cuda(cudaError_t e, const char* what);
 int fail_argument(const std::string& msg);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
-int launch_emax(const void* x, int64_t n, int* out, cudaStream_t s);
 
 namespace {
 
@@ -55,7 +59,7 @@ constexpr int kHeaderFloats = 64;   // exponent word, padded to 256 bytes
 constexpr int kScratchFloats = kHeaderFloats + 4 * kTableEntries;
 constexpr int kMaxDevices = 64;
 
-// [0]: exponent word (int); from float 64 on: tables, the one of length M at
+// [0]: exponent word (int, written, never read for results); from float 64 on: tables, the one of length M at
 // entry offset M - 32, entries (re.hi, re.lo, im.hi, im.lo).
 static __device__ __align__(256) float g_noalloc_scratch[kScratchFloats];
 
@@ -130,9 +134,6 @@ extern "C" int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* ou
   int* emax = reinterpret_cast<int*>(base);
   const float* tw = base + kHeaderFloats + 4 * (size_t)(n - 32);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // exponent word: cleared and recomputed from this call's input
-  rc = launch_emax(in, 2 * n * howmany, emax, s);
-  if (rc) return rc;
   FastArgs A;
   std::memset(&A, 0, sizeof(A));
   A.in = in;
@@ -145,6 +146,9 @@ extern "C" int pfgb_fft1d_noalloc(int sign, int64_t n, int64_t howmany, void* ou
   A.out_tfast = 0;
   A.scale_on = 0;
   A.in_dd = A.out_dd = 0;
+  // each line scaled by its own largest exponent; no per-line record (te)
+  A.self_scale = 1;
+  A.te = nullptr;
   A.emax_ptr = emax;
   A.nouter = 0;
   A.nt = howmany;

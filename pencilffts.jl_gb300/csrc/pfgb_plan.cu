@@ -180,6 +180,9 @@ struct pfgb_plan {
   bool query_only = false;  // plan analysed on the host only (no device memory)
   // opt-in per-launch timing: (direction, pass index, start, stop)
   bool timing = false;
+  // test of the bounded waits' give-up path (pfgb_plan_set_wait_test)
+  int wait_test = 0;
+  bool force_tma = false;
   struct Rec {
     int dir, pass;
     cudaEvent_t a, b;
@@ -846,7 +849,6 @@ int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_fx(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
-int launch_emax(const void* x, int64_t n, int* out, cudaStream_t s);
 int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_tc(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
@@ -863,7 +865,7 @@ int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
 // the plain kernel overlaps load and compute better (Float64 512^3 c2r pass
 // 1.05 ms against 1.09 ms; the TMA form's two tile buffers allow two CTAs).
 static bool tma_eligible(const pfgb_plan* P, const Pass& ps, const FastArgs& F) {
-  const bool wanted = ps.variant == 1 || (ps.variant < 0 && PFGB_FAST_TMA);
+  const bool wanted = ps.variant == 1 || (ps.variant < 0 && (PFGB_FAST_TMA || P->force_tma));
   if (!wanted || !ps.fast || F.op != OP_C2R || F.lmap_tile || F.in_sa != 1) return false;
   const int esz = F.op == OP_R2C ? P->rb : 2 * P->rb;
   const int64_t line = (int64_t)(F.op == OP_C2R ? F.n_in : (1 << ps.logm)) * esz;
@@ -1153,11 +1155,13 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       } else if (ps.tc) {
         F.total = grid;
         F.err = P->emax_dev + 1;
+        F.wait_test = P->wait_test;
         F.tcb = ps.tcb;
         rc = launch_tc(ps.logm, ps.sign, F, s);
       } else if (tma_eligible(P, ps, F)) {
         F.total = grid;
         F.err = P->emax_dev + 1;
+        F.wait_test = P->wait_test;
         rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, s)
                         : launch_fast_tma_f32(ps.logm, ps.sign, F, s);
       } else {
@@ -1497,6 +1501,14 @@ static int autotune_passes(pfgb_plan* P) {
     }
   }
   PFGB_CUDA(cudaMemset(P->emax_dev, 0, 16));  // exponent and error words
+  return PFGB_OK;
+}
+
+int pfgb_plan_set_wait_test(pfgb_plan* P, int polls, int tma) {
+  if (!P) return fail(PFGB_ERR_ARGUMENT, "null plan");
+  if (polls < 0) return fail(PFGB_ERR_ARGUMENT, "polls must be >= 0");
+  P->wait_test = polls;
+  P->force_tma = tma != 0;
   return PFGB_OK;
 }
 

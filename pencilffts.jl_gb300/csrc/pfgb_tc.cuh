@@ -194,8 +194,11 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
       tws[i] = w;
     }
   }
+  // never signalled: the give-up test's wait (FastArgs::wait_test)
+  unsigned long long* dead = bar + 2;
   if (tid == 0) {
     mbar_init(bar, 1);
+    mbar_init(dead, 1);
     *sfail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -292,11 +295,13 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
             tc_mma(tmem + b * C::K1, dA1[pr == 1] + ((b * 16 * SBO1 + kk * 256) >> 4),
                    dB1[pr == 0] + ((kk * 256) >> 4), ID1, (pr | kk) ? 1u : 0u);
       tc_commit(bar);
-      if (!mbar_wait_bounded(bar, phase)) *sfail = 1;
+      const bool ok = a.wait_test > 0 ? mbar_wait_bounded(dead, 0, a.wait_test) : mbar_wait_bounded(bar, phase);
+      if (!ok) *sfail = 1;
       tc_fence_before();
     }
     phase ^= 1;
     __syncthreads();
+    if (*sfail) break;  // the product may still run: no tensor-memory read
     tc_fence_after();
 
     // ---- twiddles, stage-2 operand: rows (k1, line), K = [re(n2) | im(n2)] ----
@@ -340,6 +345,7 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
     }
     phase ^= 1;
     __syncthreads();
+    if (*sfail) break;
     tc_fence_after();
 
     // ---- output X[line][k1 + N1 k2] ----
@@ -368,9 +374,10 @@ __global__ void __launch_bounds__(256, 2) tc_pass(const FastArgs a) {
   }
   if (tid == 0 && *sfail) {
     atomicOr(a.err, 2);
-    // a product that did not complete in time: wait for it once more
-    // (bounded) before its tensor memory is released
-    mbar_wait_bounded(bar, phase ^ 1);
+    // the product whose wait gave up (committed with parity phase ^ 1) may
+    // still write tensor memory: wait for it once more, bounded, before the
+    // memory is released; bit 4 if it still has not completed
+    if (!mbar_wait_bounded(bar, phase ^ 1)) atomicOr(a.err, 4);
   }
   __syncthreads();
   if (warp == 0) {

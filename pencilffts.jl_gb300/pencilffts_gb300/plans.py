@@ -354,12 +354,22 @@ class PencilFFTPlan:
 
     def device_status(self):
         """Bits set by bounded device waits that gave up since the last call
-        (1: TMA tile copy, 2: tensor-core product); synchronises the plan's
-        stream and clears them."""
+        (1: TMA tile copy, 2: tensor-core product, 4: a wait for the copies or
+        products in flight gave up too); synchronises the plan's stream and
+        clears them."""
         flags = ctypes.c_int32(0)
         _lib.check(self._L.pfgb_device_status(self._handle, self._stream_ptr(), ctypes.byref(flags)),
                    "pfgb_device_status")
         return flags.value
+
+    def set_wait_test(self, polls: int, tma: bool = False):
+        """Test hook of the bounded waits' give-up path: with ``polls > 0`` the
+        first data wait of every CTA of the persistent kernels polls an
+        mbarrier that nothing signals ``polls`` times and gives up; ``tma``
+        also runs eligible c2r passes in the TMA-fed form.  ``polls=0`` and
+        ``tma=False`` restore normal execution."""
+        _lib.check(self._L.pfgb_plan_set_wait_test(self._handle, int(polls), 1 if tma else 0),
+                   "pfgb_plan_set_wait_test")
 
     def get_timing(self):
         """Per-pass event timings recorded since the last call (synchronises)."""
