@@ -30,6 +30,11 @@ enum PassOp : int {
   OP_C2R = 2,    // two Hermitian half-spectra packed in one complex DFT, m -> n
   OP_R2R_C = 3,  // real-to-real kind applied to complex data
   OP_R2R_R = 4,  // real-to-real kind applied to real data (two lines packed)
+  // register Stockham pass only: REDFT00 / RODFT00 as a complex DFT of the
+  // even / odd extension (length a power of two), on complex lines (X00C) or
+  // on two real lines packed in one complex line (X00R)
+  OP_X00C = 5,
+  OP_X00R = 6,
 };
 
 // FFTW r2r kind codes.

@@ -31,7 +31,8 @@ struct FastArgs {
   const void* in;
   void* out;
   const void* tw;  // M entries exp(-2 pi i m / M) as Cx<R>
-  int op;          // OP_C2C, OP_R2C, OP_C2R
+  int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R
+  int r2r_odd;     // OP_X00C / OP_X00R: 0 REDFT00 (even extension), 1 RODFT00 (odd)
   int n_in, n_out;
   int lmap_tile;     // lanes along the tile dimension (tile dim contiguous in input)
   int store_direct;  // store from registers with the load mapping
@@ -130,6 +131,11 @@ __device__ __forceinline__ Cx<R> mul_ik(Cx<R> y, int64_t idx, int half, int64_t 
 #ifndef PFGB_FAST_THREADS_F32_LONG
 #define PFGB_FAST_THREADS_F32_LONG 1024
 #endif
+// Operations of the fast pass that pack two real lines in one complex line.
+__host__ __device__ constexpr bool fast_packed(int op) {
+  return op == OP_R2C || op == OP_C2R || op == OP_X00R;
+}
+
 template <typename R>
 __host__ __device__ constexpr int fast_threads(int logm, int op = OP_C2C) {
   return sizeof(R) == 4 ? (logm >= 10 && op != OP_C2R ? PFGB_FAST_THREADS_F32_LONG : PFGB_FAST_THREADS_F32)
@@ -445,7 +451,7 @@ __device__ __forceinline__ int line_exponent(unsigned emx, const FastArgs& a, un
   const int q = (lanes_across_lines && !(T == fast_threads<R>(LOGM, OP))) ? (int)threadIdx.x
                 : (T == fast_threads<R>(LOGM, OP) ? 0 : p);
   if (leader && q < nvalid_cl) {
-    const int pk = a.op == OP_C2C ? 1 : 2;
+    constexpr int pk = fast_packed(OP) ? 2 : 1;
     const unsigned rest = div31(bid, a.div_tiles);
     if (a.te) a.te[t0 / pk + q + a.te_ncl * rest] = (int)e;
     if ((int)e > *reinterpret_cast<const volatile int*>(a.emax_ptr)) atomicMax(const_cast<int*>(a.emax_ptr), (int)e);
@@ -473,6 +479,31 @@ __device__ __forceinline__ Cx<R> scale_pow2(Cx<R> y, float f) {
   else return mk(y.re * f, y.im * f);
 }
 
+// Element pos of the extension (length M) of a REDFT00 line (even: x[0..n-1],
+// n = M/2 + 1, then x[n-2..1]) or of a RODFT00 line (odd: 0, x[0..n-1], 0,
+// -x[n-1..0], n = M/2 - 1): returns the input index and sets its sign s (0:
+// the element is zero).
+__device__ __forceinline__ int x00_src(int pos, int M, int odd, int& s) {
+  const int h = M >> 1;
+  if (!odd) {
+    s = 1;
+    return pos <= h ? pos : M - pos;
+  }
+  if (pos == 0 || pos == h) {
+    s = 0;
+    return 0;
+  }
+  s = pos < h ? 1 : -1;
+  return pos < h ? pos - 1 : M - pos - 1;
+}
+// Output k of a REDFT00 / RODFT00 line (k < n): the extension's DFT Z at k
+// (even), i Z at k + 1 (odd); the register position of the store-direct path
+// holds output pos (even) or pos - 1 (odd).
+template <typename R>
+__device__ __forceinline__ Cx<R> x00_out(Cx<R> z, int odd) {
+  return odd ? mul_i(z) : z;
+}
+
 // One tile of a pass: load (from `src`: the pass input in global memory, or
 // a copy of the tile's input lines in shared memory), stages, store.  `src`
 // is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
@@ -493,7 +524,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   int p, b;
   if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
 
-  const bool packed = OP != OP_C2C;
+  constexpr bool packed = fast_packed(OP);
   const int lines = packed ? 2 * TW : TW;
   const TileOrigin o = tile_origin(a, (unsigned)bid, lines);
   const int64_t t0 = o.t0, ooff = o.ooff, didx = o.didx;
@@ -559,6 +590,72 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
         const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
         v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
       }
+    }
+  } else if constexpr (OP == OP_X00C) {
+    // complex lines through the even / odd extension
+    const int odd = a.r2r_odd;
+    if (IO::kDD && IN_DD) {
+      const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        int sg;
+        const int k = x00_src(b + r * T, M, odd, sg);
+        const float4 q = (p < nvalid && sg) ? in[(int64_t)k * ssa] : make_float4(0.f, 0.f, 0.f, 0.f);
+        Cx<R> y = ld_dd4<R>(q);
+        if (IO::kDD && a.te_rescale && p < nvalid && sg) y = scale_pow2(y, te_factor(a, o.tebase, t0 + p, k, emax));
+        v[r] = sg < 0 ? -y : y;
+      }
+    } else {
+      const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
+      MC raw[8];
+      int sgs[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int k = x00_src(b + r * T, M, odd, sgs[r]);
+        raw[r] = (p < nvalid && sgs[r]) ? in[(int64_t)k * ssa] : MC{0, 0};
+      }
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
+          emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax_out = emax + a.emax_shift;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const Cx<R> y = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
+        v[r] = sgs[r] < 0 ? -y : y;
+      }
+    }
+  } else if constexpr (OP == OP_X00R) {
+    // two real lines (2p, 2p + 1) through the even / odd extension; double input
+    const int odd = a.r2r_odd;
+    const MR* in = reinterpret_cast<const MR*>(src) + ioff;
+    const int i0 = 2 * p, i1 = 2 * p + 1;
+    MR ra[8], rb[8];
+    int sgs[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int k = x00_src(b + r * T, M, odd, sgs[r]);
+      const int64_t off = (int64_t)k * ssa;
+      ra[r] = (i0 < nvalid && sgs[r]) ? in[off + (int64_t)i0 * sst] : MR(0);
+      rb[r] = (i1 < nvalid && sgs[r]) ? in[off + (int64_t)i1 * sst] : MR(0);
+    }
+    if constexpr (IO::kDD) {
+      if (a.self_scale) {
+        unsigned emx = 0;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
+        emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+        emax_out = emax + a.emax_shift;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const Cx<R> y = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
+      v[r] = sgs[r] < 0 ? -y : y;
     }
   } else if constexpr (OP == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
@@ -666,6 +763,38 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
           }
         }
       }
+    } else if constexpr (OP == OP_X00C) {
+      // outputs k < n: register r holds k = pos (even) or pos - 1 (odd)
+      const int odd = a.r2r_odd, n = a.n_out;
+      if (p < nvalid) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          const int k = b + r * T - odd;
+          if (k < 0 || k >= n) continue;
+          const Cx<R> y = apply_scale(x00_out(v[r], odd), a);
+          if (IO::kDD && OUT_DD) {
+            reinterpret_cast<float4*>(a.out)[ooff + (int64_t)p * a.out_st + (int64_t)k * a.out_sa] = st_dd4(y);
+          } else {
+            MC o;
+            o.x = outr<R>(y.re, emax_out);
+            o.y = outr<R>(y.im, emax_out);
+            reinterpret_cast<MC*>(a.out)[ooff + (int64_t)p * a.out_st + (int64_t)k * a.out_sa] = o;
+          }
+        }
+      }
+    } else if constexpr (OP == OP_X00R) {
+      const int odd = a.r2r_odd, n = a.n_out;
+      MR* out = reinterpret_cast<MR*>(a.out) + ooff;
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int k = b + r * T - odd;
+        if (k < 0 || k >= n) continue;
+        const Cx<R> y = apply_scale(x00_out(v[r], odd), a);
+        const int64_t off = (int64_t)k * a.out_sa;
+        if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax_out);
+        if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, emax_out);
+      }
     } else {  // C2R, real outputs of lines 2p and 2p+1
       MR* out = reinterpret_cast<MR*>(a.out) + ooff;
       const int i0 = 2 * p, i1 = 2 * p + 1;
@@ -755,6 +884,39 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
           out[off + (int64_t)i1 * a.out_st] = o;
         }
       }
+    }
+  } else if constexpr (OP == OP_X00C) {
+    const int odd = a.r2r_odd, n = a.n_out;
+    MC* out = reinterpret_cast<MC*>(a.out) + ooff;
+    const int tot = TW * n;
+    for (int e = tid; e < tot; e += nth) {
+      int i, k;
+      if (a.out_tfast) { i = e % TW; k = e / TW; } else { k = e % n; i = e / n; }
+      if (i >= nvalid) continue;
+      const Cx<R> y = apply_scale(x00_out(z[sidx<R, LOGM, OP>(i, k + odd)], odd), a);
+      if (IO::kDD && OUT_DD) {
+        reinterpret_cast<float4*>(out)[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = st_dd4(y);
+      } else {
+        const int eo = line_emax_out(i);
+        MC o;
+        o.x = outr<R>(y.re, eo);
+        o.y = outr<R>(y.im, eo);
+        out[(int64_t)k * a.out_sa + (int64_t)i * a.out_st] = o;
+      }
+    }
+  } else if constexpr (OP == OP_X00R) {
+    const int odd = a.r2r_odd, n = a.n_out;
+    MR* out = reinterpret_cast<MR*>(a.out) + ooff;
+    const int tot = TW * n;
+    for (int e = tid; e < tot; e += nth) {
+      int q, k;
+      if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % n; q = e / n; }
+      const Cx<R> y = apply_scale(x00_out(z[sidx<R, LOGM, OP>(q, k + odd)], odd), a);
+      const int i0 = 2 * q, i1 = 2 * q + 1;
+      const int64_t off = (int64_t)k * a.out_sa;
+      const int eo = line_emax_out(q);
+      if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, eo);
+      if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
     }
   } else {  // C2R with a transposed output layout
     MR* out = reinterpret_cast<MR*>(a.out) + ooff;

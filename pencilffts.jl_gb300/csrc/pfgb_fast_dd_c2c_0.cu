@@ -10,6 +10,11 @@ int launch_fast_dd_r2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cu
 int launch_fast_dd_r2c_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_c2r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_c2r_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_x00c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_x00c_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_x00c_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_x00c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_x00r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
 int launch_fast_dd_c2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   return launch_fast_op<dd, OP_C2C, 0>(logm, sign, A, grid, s);
@@ -28,6 +33,11 @@ int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStre
     case OP_R2C * 4 + 2: return launch_fast_dd_r2c_2(logm, sign, A, grid, s);
     case OP_C2R * 4 + 0: return launch_fast_dd_c2r_0(logm, sign, A, grid, s);
     case OP_C2R * 4 + 1: return launch_fast_dd_c2r_1(logm, sign, A, grid, s);
+    case OP_X00C * 4 + 0: return launch_fast_dd_x00c_0(logm, sign, A, grid, s);
+    case OP_X00C * 4 + 1: return launch_fast_dd_x00c_1(logm, sign, A, grid, s);
+    case OP_X00C * 4 + 2: return launch_fast_dd_x00c_2(logm, sign, A, grid, s);
+    case OP_X00C * 4 + 3: return launch_fast_dd_x00c_3(logm, sign, A, grid, s);
+    case OP_X00R * 4 + 0: return launch_fast_dd_x00r_0(logm, sign, A, grid, s);
     default: return PFGB_ERR_UNSUPPORTED;
   }
 }

@@ -51,6 +51,13 @@ static int launch_fast_op(int logm, int sign, const FastArgs& A, int64_t grid, c
                   : launch_fast_sign<R, 1, OP, IOM>(logm, A, grid, s);
 }
 
+// Operations that only run with the forward sign (REDFT00 / RODFT00 through
+// their extensions, which are real-symmetric in the sign)
+template <typename R, int OP, int IOM>
+static int launch_fast_op_fwd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return sign < 0 ? launch_fast_sign<R, -1, OP, IOM>(logm, A, grid, s) : PFGB_ERR_UNSUPPORTED;
+}
+
 // TMA-fed persistent form (c2r passes); A.total == 0 only configures it.
 template <typename R, int LOGM, int SIGN, int IOM>
 static int launch_tma_one(const FastArgs& A, cudaStream_t s) {

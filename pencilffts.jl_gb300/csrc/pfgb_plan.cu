@@ -104,8 +104,11 @@ struct Pass {
   const void* chirp = nullptr;
   const void* bfilt = nullptr;
   const void* r2rtw = nullptr;
-  // register Stockham kernel for power-of-two lines (fast_pass)
+  // register Stockham kernel for power-of-two lines (fast_pass) and its
+  // operation (OP_C2C, OP_R2C, OP_C2R, or OP_X00C / OP_X00R for REDFT00 and
+  // RODFT00 through their power-of-two extensions)
   bool fast = false;
+  int fop = -1;
   // Float64 fast passes: dd-form input / output between consecutive dd passes,
   // and an exponent reduction over the input before the first pass of a run
   bool in_dd = false, out_dd = false, reduce_before = false;
@@ -533,22 +536,28 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   }
   int rc = prepare_core(P, ps, M);
   if (rc) return rc;
-  // power-of-two c2c / r2c / c2r lines take the register Stockham kernel; on
-  // Float64 plans it computes in dd unless native FP64 was requested
-  if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && ps.L == 0 && M >= 8 &&
+  // power-of-two c2c / r2c / c2r lines, and REDFT00 / RODFT00 lines whose
+  // extension has a power-of-two length (n = 2^k + 1, 2^k - 1), take the
+  // register Stockham kernel; on Float64 plans it computes in dd unless
+  // native FP64 was requested (block floating point plans keep the R2R kinds
+  // on the generic kernel)
+  const bool x00 = (ps.op == OP_R2R_C || ps.op == OP_R2R_R) &&
+                   (ps.r2r_kind == K_REDFT00 || ps.r2r_kind == K_RODFT00) && !P->fx;
+  if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R || x00) && ps.L == 0 && M >= 8 &&
       M <= 4096 && (M & (M - 1)) == 0 &&
       !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
     ps.fast = true;
+    ps.fop = x00 ? (ps.op == OP_R2R_C ? OP_X00C : OP_X00R) : ps.op;
     ps.logm = 0;
     while ((1 << ps.logm) < M) ++ps.logm;
     rc = upload_fast_table(P, M, &ps.ftw);
     if (!rc && P->fx) rc = upload_fast_table_fx(P, M, ps.sign, &ps.ftw_fx);
     if (rc) return rc;
-    const bool packed = ps.op != OP_C2C;
-    ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.op) : fast_tw<float>(ps.logm, ps.op);
+    const bool packed = fast_packed(ps.fop);
+    ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.fop) : fast_tw<float>(ps.logm, ps.fop);
     ps.lines = packed ? 2 * ps.clines : ps.clines;
-    ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm, ps.op) : fast_threads<float>(ps.logm, ps.op);
-    ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm, ps.op) : fast_smem<float>(ps.logm, ps.op);
+    ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm, ps.fop) : fast_threads<float>(ps.logm, ps.fop);
+    ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm, ps.fop) : fast_smem<float>(ps.logm, ps.fop);
     if (P->precision == PFGB_PRECISION_TC_SPLIT && ps.op == OP_C2C && tc_lines(ps.logm) > 0) {
       ps.tc = true;
       ps.clines = ps.lines = tc_lines(ps.logm);
@@ -603,7 +612,7 @@ static int tile_dim(const Pass& ps) {
 static int64_t complex_lines(const Pass& ps) {
   const int t = tile_dim(ps);
   const int64_t nt = t >= 0 ? ps.lin.size[t] : 1;
-  return ps.op == OP_C2C ? nt : (nt + 1) / 2;
+  return fast_packed(ps.fop) ? (nt + 1) / 2 : nt;
 }
 
 // Element -> first-pass line map of the second pass of a Float64 run: the
@@ -614,7 +623,7 @@ static int64_t complex_lines(const Pass& ps) {
 // number of p1's complex lines.
 static int64_t te_mapping(const Pass& p1, Pass& p2) {
   const int a1 = p1.axis, t1 = tile_dim(p1);
-  const int sh1 = p1.op == OP_C2C ? 0 : 1;
+  const int sh1 = fast_packed(p1.fop) ? 1 : 0;
   const int64_t ncl1 = complex_lines(p1);
   int64_t mul1[kMaxD] = {};
   int64_t m = ncl1;
@@ -751,7 +760,8 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.in = in;
   F.out = out;
   F.tw = ps.ftw;
-  F.op = ps.op;
+  F.op = ps.fop;
+  F.r2r_odd = ps.r2r_kind == K_RODFT00 ? 1 : 0;
   F.n_in = A.n_in;
   F.n_out = A.n_out;
   F.lmap_tile = A.in_tfast;
@@ -1330,10 +1340,13 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
   if (!rc && P->rb == 8) {
     for (auto* dir : {&P->fwd, &P->bwd}) {
       auto& v = dir->passes;
+      // passes that exchange dd-form data with their neighbours (packed real
+      // R2R lines always read and write doubles)
+      auto chains = [](const Pass& q) { return q.fast && q.fop != OP_X00R; };
       for (size_t i = 0; i < v.size(); ++i) {
         if (!v[i].fast) continue;
-        const bool prev = i > 0 && v[i - 1].fast;
-        const bool next = i + 1 < v.size() && v[i + 1].fast;
+        const bool prev = chains(v[i]) && i > 0 && chains(v[i - 1]);
+        const bool next = chains(v[i]) && i + 1 < v.size() && chains(v[i + 1]);
         v[i].in_dd = prev;
         v[i].out_dd = next;
         v[i].reduce_before = !prev;
@@ -1361,7 +1374,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
         if (ps.fast) {
           FastArgs F;
           std::memset(&F, 0, sizeof(F));
-          F.op = ps.op;
+          F.op = ps.fop;
           F.in_dd = ps.in_dd ? 1 : 0;  // selects the kernel variant
           F.out_dd = ps.out_dd ? 1 : 0;
           rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
