@@ -174,6 +174,21 @@ int pfgb_forward_deriv(pfgb_plan* plan, void* dst, const void* src, void* stream
 int pfgb_backward_deriv(pfgb_plan* plan, void* dst, const void* src, void* stream, int normalise,
                         int dim, double length);
 
+/* Sum of spectral derivatives of several fields in one backward transform:
+ *   dst = plan \ (sum_t coef[t] * i k_{dim[t]} * src[t]),  1 <= nterm <= 3,
+ * with k as in pfgb_backward_deriv (length[t]: domain length along dim[t]);
+ * bmul! when normalise == 0.  Replaces the reference's vector calculus in
+ * Fourier space followed by one ldiv! per result (divergence and curl!,
+ * test/include/FourierOperations.jl:18-86; examples/gradient.jl:48-318): the
+ * divergence of u is the three terms (u1, 0, 1), (u2, 1, 1), (u3, 2, 1), and
+ * curl component 1 is (u3, 1, 1), (u2, 2, -1).  The sources, which have the
+ * plan's output layout, are read once by the first backward pass (a
+ * complex-to-complex pass, as for pfgb_backward_deriv) and not modified; the
+ * other passes are those of pfgb_backward.  Out-of-place plans only. */
+int pfgb_backward_deriv_sum(pfgb_plan* plan, void* dst, const void* const* src, int nterm,
+                            const int* dim, const double* coef, const double* length,
+                            void* stream, int normalise);
+
 /* Applies one plan to a collection of arrays (reference mul!/ldiv!/bmul!
  * broadcast over tuples or arrays of PencilArrays, src/operations.jl:129-152).
  * direction: +1 forward, -1 backward; normalise as in pfgb_backward. */

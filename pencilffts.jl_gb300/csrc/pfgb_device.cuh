@@ -22,6 +22,7 @@ namespace pfgb {
 constexpr int kMaxStages = 8;
 constexpr int kMaxDevicesConfigured = 64;  // devices per process the launchers track
 constexpr int kMaxOuter = 12;
+constexpr int kMaxTerms = 3;  // sources of a fused sum of spectral derivatives
 
 // Operation performed by a pass.
 enum PassOp : int {
@@ -35,6 +36,9 @@ enum PassOp : int {
   // on two real lines packed in one complex line (X00R)
   OP_X00C = 5,
   OP_X00R = 6,
+  // register Stockham pass only: a c2c pass whose input is the sum over up
+  // to kMaxTerms sources of c_t i k_t src_t (fused divergence / curl)
+  OP_CSUM = 7,
 };
 
 // FFTW r2r kind codes.
@@ -74,6 +78,15 @@ struct PassArgs {
   int deriv, deriv_role, deriv_half;
   int64_t deriv_n;
   double k0;
+  // fused sum of spectral derivatives (c2c passes, nterm > 0): the input of
+  // the pass is sum_t i k_t(idx) tsrc[t], k_t = tk0[t] f with f the
+  // frequency of the index along the dimension of role trole[t] (0 axis, 1
+  // tile dimension, 2 + o outer dimension o); tsrc[t] has the layout of in
+  int nterm;
+  const void* tsrc[kMaxTerms];
+  int trole[kMaxTerms], thalf[kMaxTerms];
+  int64_t tn[kMaxTerms];
+  double tk0[kMaxTerms];
 };
 
 template <typename R>
@@ -438,16 +451,24 @@ __global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
   const int64_t t0 = tile * a.lines;
   int64_t ioff = t0 * a.in_st, ooff = t0 * a.out_st;
   int64_t didx = 0;
+  int64_t tdidx[kMaxTerms] = {0, 0, 0};
   for (int d = 0; d < a.nouter; ++d) {
     const int64_t idx = rest % a.osz[d];
     rest /= a.osz[d];
     ioff += idx * a.in_so[d];
     ooff += idx * a.out_so[d];
     if (a.deriv && a.deriv_role == 2 + d) didx = idx;
+    for (int t = 0; t < a.nterm; ++t)
+      if (a.trole[t] == 2 + d) tdidx[t] = idx;
   }
   auto ik = [&](Cx<R> y, int64_t idx) {
     const int64_t f = (a.deriv_half || idx <= (a.deriv_n - 1) / 2) ? idx : idx - a.deriv_n;
     const R k = R(a.k0 * (double)f);
+    return mk(-(y.im * k), y.re * k);
+  };
+  auto ik_t = [&](int t, Cx<R> y, int64_t idx) {
+    const int64_t f = (a.thalf[t] || idx <= (a.tn[t] - 1) / 2) ? idx : idx - a.tn[t];
+    const R k = R(a.tk0[t] * (double)f);
     return mk(-(y.im * k), y.re * k);
   };
   const int nvalid = (int)min((int64_t)a.lines, a.nt - t0);
@@ -468,7 +489,14 @@ __global__ void __launch_bounds__(1024) pass_kernel(const PassArgs a) {
       int i, j;
       if (a.in_tfast) { i = e % a.lines; j = e / a.lines; } else { j = e % a.n_in; i = e / a.n_in; }
       Cx<R> x = mk(R(0), R(0));
-      if (i < nvalid) x = in[(int64_t)j * a.in_sa + (int64_t)i * a.in_st];
+      if (a.nterm > 0) {
+        for (int t = 0; t < a.nterm && i < nvalid; ++t) {
+          const Cx<R> y = reinterpret_cast<const Cx<R>*>(a.tsrc[t])[ioff + (int64_t)j * a.in_sa + (int64_t)i * a.in_st];
+          x = x + ik_t(t, y, a.trole[t] == 0 ? (int64_t)j : a.trole[t] == 1 ? t0 + i : tdidx[t]);
+        }
+      } else if (i < nvalid) {
+        x = in[(int64_t)j * a.in_sa + (int64_t)i * a.in_st];
+      }
       if (a.deriv == 1)
         x = ik(x, a.deriv_role == 0 ? (int64_t)j : a.deriv_role == 1 ? t0 + i : didx);
       Cx<R>* zl = z + (size_t)i * a.lp;

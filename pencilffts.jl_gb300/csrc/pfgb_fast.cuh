@@ -77,6 +77,14 @@ struct FastArgs {
   int deriv, deriv_role, deriv_half;
   int64_t deriv_n;  // physical length of the dimension (frequency wrap)
   float k0_h, k0_l;
+  // OP_CSUM: the pass input is sum_t i k_t(idx) tsrc[t] (k_t = tk0[t] f, f
+  // the frequency along the dimension of role trole[t], as deriv_role); the
+  // sources have the layout of the pass input
+  int nterm;
+  const void* tsrc[kMaxTerms];
+  int trole[kMaxTerms], thalf[kMaxTerms];
+  int64_t tn[kMaxTerms];
+  float tk0_h[kMaxTerms], tk0_l[kMaxTerms];
   // persistent forms (fast_pass_tma, tc_pass): tiles of the pass and an error
   // word set when a bounded wait gives up
   int64_t total;
@@ -467,6 +475,13 @@ __device__ __forceinline__ unsigned dexp_u(double x) {
 __device__ __forceinline__ unsigned te_index(const FastArgs& a, unsigned tebase, int64_t line, int pos) {
   return tebase + ((unsigned)line >> a.te_sh[1]) * a.te_mul[1] + ((unsigned)pos >> a.te_sh[0]) * a.te_mul[0];
 }
+// Index along outer dimension d of tile `bid` (the multiply-and-shift decode
+// of tile_origin).
+__device__ __forceinline__ int64_t outer_index(const FastArgs& a, unsigned bid, int d) {
+  unsigned rest = div31(bid, a.div_tiles);
+  for (int q = 0; q < d; ++q) rest = div31(rest, a.div_osz[q]);
+  return (int64_t)(rest - div31(rest, a.div_osz[d]) * (unsigned)a.osz[d]);
+}
 __device__ __forceinline__ float pow2_le0(int d) {
   return d >= -126 ? __uint_as_float((unsigned)(d + 127) << 23) : 0.0f;
 }
@@ -589,6 +604,40 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       for (int r = 0; r < 8; ++r) {
         const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
         v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
+      }
+    }
+  } else if constexpr (OP == OP_CSUM) {
+    // sum over the terms of i k_t(idx) src_t, converted with one line
+    // exponent over all terms (first loop: exponents only; second: values)
+    int64_t tidx[kMaxTerms];
+#pragma unroll
+    for (int t = 0; t < kMaxTerms; ++t)
+      tidx[t] = (t < a.nterm && a.trole[t] >= 2) ? outer_index(a, (unsigned)bid, a.trole[t] - 2) : 0;
+    if constexpr (IO::kDD) {
+      if (a.self_scale) {
+        unsigned emx = 0;
+        for (int t = 0; t < a.nterm; ++t) {
+          const MC* in = reinterpret_cast<const MC*>(a.tsrc[t]) + ioff + (int64_t)p * sst;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const MC q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
+            emx = max(emx, max(dexp_u(q.x), dexp_u(q.y)));
+          }
+        }
+        emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+        emax_out = emax + a.emax_shift;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = mk(R(0), R(0));
+    for (int t = 0; t < a.nterm; ++t) {
+      const MC* in = reinterpret_cast<const MC*>(a.tsrc[t]) + ioff + (int64_t)p * sst;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const MC q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
+        const int64_t idx = a.trole[t] == 0 ? (int64_t)(b + r * T) : a.trole[t] == 1 ? t0 + p : tidx[t];
+        v[r] = v[r] + mul_ik(mk(mkr<R>(q.x, emax), mkr<R>(q.y, emax)), idx, a.thalf[t], a.tn[t],
+                             a.tk0_h[t], a.tk0_l[t]);
       }
     }
   } else if constexpr (OP == OP_X00C) {
@@ -745,7 +794,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     }
   }
   if (a.store_direct && OP != OP_R2C) {
-    if constexpr (OP == OP_C2C) {
+    if constexpr (OP == OP_C2C || OP == OP_CSUM) {
       if (p < nvalid) {
         if (IO::kDD && OUT_DD) {
           float4* out = reinterpret_cast<float4*>(a.out) + ooff + (int64_t)p * a.out_st;
@@ -826,7 +875,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   // output exponent of complex line i (the first pass of a run scales lines
   // separately; the loops below write other threads' lines)
   auto line_emax_out = [&](int i) { return IO::kDD && a.self_scale ? lexp[i] + a.emax_shift : emax_out; };
-  if constexpr (OP == OP_C2C) {
+  if constexpr (OP == OP_C2C || OP == OP_CSUM) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
     const int tot = TW * M;
     for (int e = tid; e < tot; e += nth) {

@@ -149,6 +149,13 @@ struct Deriv {
   int64_t n = 0;  // physical length along dim
   int half = 0;   // 1 along the half-spectrum dimension of r2c / c2r plans
   double k0 = 0;
+  // mode 3: the input of the first backward pass is sum_t i k_t src[t] over
+  // nterm sources (k_t = tk0[t] f along logical dimension tdim[t])
+  int nterm = 0;
+  const void* tsrc[kMaxTerms] = {};
+  int tdim[kMaxTerms] = {}, thalf[kMaxTerms] = {};
+  int64_t tn[kMaxTerms] = {};
+  double tk0[kMaxTerms] = {};
 };
 
 }  // namespace pfgb
@@ -725,19 +732,32 @@ static int make_args(const pfgb_plan* P, const Pass& ps, const void* in, void* o
   }
   A.nouter = no;
   grid = nblocks;
-  if (dv && dv->mode) {
-    int role = -1;
-    if (dv->dim == a) role = 0;
-    else if (dv->dim == t) role = 1;
-    else {
-      int o = 0;
-      for (int q = 0; q < D; ++q) {
-        const int d = ps.lin.perm[q];
-        if (d == a || d == t) continue;
-        if (d == dv->dim) role = 2 + o;
-        ++o;
-      }
+  // role of logical dimension dim in this pass: 0 axis, 1 tile, 2 + o outer
+  auto role_of = [&](int dim) {
+    if (dim == a) return 0;
+    if (dim == t) return 1;
+    int o = 0;
+    for (int q = 0; q < D; ++q) {
+      const int d = ps.lin.perm[q];
+      if (d == a || d == t) continue;
+      if (d == dim) return 2 + o;
+      ++o;
     }
+    return -1;
+  };
+  if (dv && dv->mode == 3) {
+    A.nterm = dv->nterm;
+    for (int k = 0; k < dv->nterm; ++k) {
+      const int role = role_of(dv->tdim[k]);
+      if (role < 0) return fail(PFGB_ERR_ARGUMENT, "derivative dimension not found in the pass");
+      A.tsrc[k] = dv->tsrc[k];
+      A.trole[k] = role;
+      A.thalf[k] = dv->thalf[k];
+      A.tn[k] = dv->tn[k];
+      A.tk0[k] = dv->tk0[k];
+    }
+  } else if (dv && dv->mode) {
+    const int role = role_of(dv->dim);
     if (role < 0) return fail(PFGB_ERR_ARGUMENT, "derivative dimension not found in the pass");
     A.deriv = dv->mode;
     A.deriv_role = role;
@@ -809,6 +829,19 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
     F.self_scale = 0;
     F.te_rescale = 0;
     F.te = nullptr;
+  }
+  if (A.nterm > 0) {
+    if (ps.fop != OP_C2C) return fail(PFGB_ERR_UNSUPPORTED, "internal: derivative sum on a non-c2c pass");
+    F.op = OP_CSUM;
+    F.nterm = A.nterm;
+    for (int k = 0; k < A.nterm; ++k) {
+      F.tsrc[k] = A.tsrc[k];
+      F.trole[k] = A.trole[k];
+      F.thalf[k] = A.thalf[k];
+      F.tn[k] = A.tn[k];
+      F.tk0_h[k] = (float)A.tk0[k];
+      F.tk0_l[k] = (float)((ld)A.tk0[k] - (ld)F.tk0_h[k]);
+    }
   }
   F.deriv = A.deriv;
   F.deriv_role = A.deriv_role;
@@ -1120,6 +1153,8 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       if (first_tr < 0) first_tr = i;
     }
   const int dpass = dv && dv->mode ? (dv->mode == 2 ? last_tr : first_tr) : -1;
+  if (dv && dv->mode == 3 && dpass != 0)
+    return fail(PFGB_ERR_UNSUPPORTED, "a sum of derivatives needs the first backward pass to be a transform");
   // Float64 fast passes: fx, or dd for an execution with a fused derivative
   const bool fxrun = P->fx && !(dv && dv->mode);
   if (dv && dv->mode) {
@@ -1738,6 +1773,31 @@ int pfgb_backward_deriv(pfgb_plan* P, void* dst, const void* src, void* stream, 
   rc = make_deriv(P, 1, dim, length, dv);
   if (rc) return rc;
   return execute(P, P->bwd, dst, src, (cudaStream_t)stream, normalise != 0, -1, &dv);
+}
+
+int pfgb_backward_deriv_sum(pfgb_plan* P, void* dst, const void* const* src, int nterm, const int* dim,
+                            const double* coef, const double* length, void* stream, int normalise) {
+  if (!P) return fail(PFGB_ERR_ARGUMENT, "null plan");
+  if (nterm < 1 || nterm > kMaxTerms)
+    return fail(PFGB_ERR_ARGUMENT, "a sum of derivatives takes 1 to " + std::to_string(kMaxTerms) + " terms");
+  if (!src || !dim || !coef || !length) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  if (P->inplace) return fail(PFGB_ERR_ARGUMENT, "a sum of derivatives needs an out-of-place plan");
+  Deriv dv;
+  dv.mode = 3;
+  dv.nterm = nterm;
+  for (int k = 0; k < nterm; ++k) {
+    int rc = check_buffers(P, dst, src[k], false);
+    if (rc) return rc;
+    Deriv one;
+    rc = make_deriv(P, 1, dim[k], length[k], one);
+    if (rc) return rc;
+    dv.tsrc[k] = src[k];
+    dv.tdim[k] = one.dim;
+    dv.thalf[k] = one.half;
+    dv.tn[k] = one.n;
+    dv.tk0[k] = coef[k] * one.k0;
+  }
+  return execute(P, P->bwd, dst, src[0], (cudaStream_t)stream, normalise != 0, -1, &dv);
 }
 
 int pfgb_execute_many(pfgb_plan* P, int direction, int normalise, void* const* dst,

@@ -9,11 +9,13 @@ from ._lib import ArgumentError, LibraryError, load as load_library
 from .plans import (FFTW_ESTIMATE, FFTW_EXHAUSTIVE, FFTW_MEASURE, FFTW_PATIENT, Batch,
                     ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
                     allocate_input, allocate_output, bmul_, gather, is_inplace,
-                    ldiv, ldiv_, mul_, plan_query, scale_factor)
+                    ldiv, ldiv_, ldiv_curl_, ldiv_deriv_sum_, ldiv_divergence_, mul_,
+                    plan_query, scale_factor)
 
 __all__ = [
     "Transforms", "Batch", "ArgumentError", "LibraryError", "load_library", "ManyPencilArray",
     "Pencil", "PencilArray", "PencilFFTPlan", "Val", "allocate_input", "allocate_output",
-    "bmul_", "gather", "is_inplace", "ldiv", "ldiv_", "mul_", "plan_query", "scale_factor",
+    "bmul_", "gather", "is_inplace", "ldiv", "ldiv_", "ldiv_curl_", "ldiv_deriv_sum_",
+    "ldiv_divergence_", "mul_", "plan_query", "scale_factor",
     "FFTW_ESTIMATE", "FFTW_MEASURE", "FFTW_PATIENT", "FFTW_EXHAUSTIVE",
 ]

@@ -83,6 +83,9 @@ SIGNATURES = {
     "pfgb_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
     "pfgb_forward_deriv": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_double]),
     "pfgb_backward_deriv": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    "pfgb_backward_deriv_sum": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(_vp), ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(ctypes.c_double), _vp, ctypes.c_int]),
     "pfgb_execute_many": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp),
                                          ctypes.POINTER(_vp), ctypes.c_int, _vp]),
     "pfgb_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.POINTER(ctypes.c_int),

@@ -26,7 +26,8 @@ SOURCES = ["pfgb_plan.cu", "pfgb_kernels.cu", "pfgb_noalloc.cu", "pfgb_tc.cu"] +
     f"pfgb_fast_f32_{op}.cu" for op in ("c2c", "r2c", "c2r", "x00")] + [
     f"pfgb_fast_{t}_{op}_{iom}.cu" for t in ("dd", "fx")
     for op, ioms in (("c2c", (0, 1, 2, 3)), ("r2c", (0, 2)), ("c2r", (0, 1))) for iom in ioms] + [
-    f"pfgb_fast_dd_x00c_{iom}.cu" for iom in (0, 1, 2, 3)] + ["pfgb_fast_dd_x00r_0.cu"]
+    f"pfgb_fast_dd_x00c_{iom}.cu" for iom in (0, 1, 2, 3)] + ["pfgb_fast_dd_x00r_0.cu"] + [
+    f"pfgb_fast_dd_csum_{iom}.cu" for iom in (0, 2)]
 
 
 def _nvcc():

@@ -632,6 +632,60 @@ def ldiv_(dst, plan: PencilFFTPlan, src, *, deriv=None):
     return _apply(dst, plan, src, False, True, deriv)
 
 
+def ldiv_deriv_sum_(dst, plan: PencilFFTPlan, terms, *, normalise=True):
+    """``dst = plan \\ (sum of coef * i k_dim * src)`` in one backward transform.
+
+    ``terms`` is a sequence of 1 to 3 tuples ``(src, dim, coef, L)``: a
+    spectral array (the plan's output), the 1-based dimension of the
+    derivative, its coefficient and the domain length along ``dim``.  The
+    sum is formed as the first backward pass reads the sources (which are
+    not modified), so a divergence or a curl component costs one backward
+    transform (reference: the Fourier-space ``divergence`` and ``curl!`` of
+    test/include/FourierOperations.jl:18-86, each followed by ``ldiv!``).
+    ``normalise=False`` gives ``bmul!`` instead of ``ldiv!``.
+    """
+    terms = list(terms)
+    if not 1 <= len(terms) <= 3:
+        raise ArgumentError("a sum of derivatives takes 1 to 3 terms")
+    n = len(terms)
+    srcs = (ctypes.c_void_p * n)()
+    dims = (ctypes.c_int * n)()
+    coefs = (ctypes.c_double * n)()
+    lens = (ctypes.c_double * n)()
+    for i, (src, dim, coef, L) in enumerate(terms):
+        if not 1 <= int(dim) <= plan.ndims:
+            raise ArgumentError(f"derivative dimension {dim} not in 1:{plan.ndims}")
+        plan._check_arrays(dst, src)
+        srcs[i] = src.data_ptr()
+        dims[i] = int(dim) - 1
+        coefs[i] = float(coef)
+        lens[i] = float(L)
+    rc = plan._L.pfgb_backward_deriv_sum(plan._handle, ctypes.c_void_p(dst.data_ptr()), srcs, n, dims,
+                                         coefs, lens, plan._stream_ptr(), 1 if normalise else 0)
+    _lib.check(rc, "pfgb_backward_deriv_sum")
+    return dst
+
+
+def ldiv_divergence_(dst, plan: PencilFFTPlan, uF, lengths):
+    """Physical divergence of the vector field whose spectrum is ``uF`` (one
+    spectral array per dimension): one fused backward transform."""
+    if len(uF) != plan.ndims or len(lengths) != plan.ndims:
+        raise ArgumentError("divergence: one component and one domain length per dimension")
+    return ldiv_deriv_sum_(dst, plan, [(uF[d], d + 1, 1.0, lengths[d]) for d in range(plan.ndims)])
+
+
+def ldiv_curl_(omega, plan: PencilFFTPlan, uF, lengths):
+    """Physical curl of the 3D vector field whose spectrum is ``uF``:
+    ``omega[a] = d_b u_c - d_c u_b`` for (a, b, c) cyclic, one fused backward
+    transform per component (reference curl!, test/include/FourierOperations.jl:57-86)."""
+    if plan.ndims != 3 or len(uF) != 3 or len(omega) != 3 or len(lengths) != 3:
+        raise ArgumentError("curl: a 3D plan with three components and three domain lengths")
+    for a in range(3):
+        b, c = (a + 1) % 3, (a + 2) % 3
+        ldiv_deriv_sum_(omega[a], plan, [(uF[c], b + 1, 1.0, lengths[b]), (uF[b], c + 1, -1.0, lengths[c])])
+    return omega
+
+
 def bmul_(dst, plan: PencilFFTPlan, src, *, deriv=None):
     """``bmul!(dst, plan, src)``: unnormalised backward transform (operations.jl:34-41)."""
     return _apply(dst, plan, src, False, False, deriv)

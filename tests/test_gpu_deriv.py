@@ -109,3 +109,77 @@ def test_derivative_errors(cuda):
     planb = P.PencilFFTPlan((16, 12, 9), T.BRFFT(16), np.float64)
     with pytest.raises(P.LibraryError, match="complex-to-complex"):
         P.mul_(planb.allocate_output(), planb, planb.allocate_input(), deriv=(1, 1.0))
+
+
+# -- fused sums of derivatives: divergence and curl in one backward transform each --
+@pytest.mark.parametrize("real", [np.float64, np.float32])
+@pytest.mark.parametrize("dims,tr", [((64, 32, 48), T.RFFT()), ((32, 24, 40), T.FFT()),
+                                     ((30, 20, 12), T.RFFT()), ((16, 64, 8), T.RFFT())],
+                         ids=["rfft-pow2", "fft", "rfft-generic", "rfft-tiles"])
+def test_fused_divergence_and_curl_match_oracle(cuda, dims, tr, real):
+    """dst = plan \\ sum_t c_t i k_t uF_t against the oracle, for the
+    divergence (three terms) and the three curl components (two terms each),
+    on power-of-two (register kernel) and generic first backward passes."""
+    plan = P.PencilFFTPlan(dims, tr, real)
+    orc = oracle_plan(plan)
+    rng = np.random.default_rng(21)
+    L = (2 * np.pi, 3.0, 5.5)
+    specs = [orc.forward(random_input(plan, 30 + c)) for c in range(3)]
+    uF = []
+    for s in specs:
+        S = plan.allocate_output()
+        S.copy_from_logical(s)
+        uF.append(S)
+    before = [S.to_logical() for S in uF]
+    ik = [O.wavenumbers(orc, d, L[d]) for d in range(3)]
+    tol = TOL[np.dtype(real)]
+    div = plan.allocate_input()
+    P.ldiv_divergence_(div, plan, uF, L)
+    ref = orc.ldiv(ik[0] * specs[0] + ik[1] * specs[1] + ik[2] * specs[2])
+    assert rel(div.to_logical(), ref) <= tol
+    om = plan.allocate_input(P.Val(3))
+    P.ldiv_curl_(om, plan, uF, L)
+    for a in range(3):
+        b, c = (a + 1) % 3, (a + 2) % 3
+        ref = orc.ldiv(ik[b] * specs[c] - ik[c] * specs[b])
+        assert rel(om[a].to_logical(), ref) <= tol, a
+    for S, b0 in zip(uF, before):
+        assert np.array_equal(S.to_logical(), b0)  # sources untouched
+    # bmul! form and a single term with a coefficient
+    U = plan.allocate_input()
+    P.ldiv_deriv_sum_(U, plan, [(uF[1], 2, -2.5, L[1])], normalise=False)
+    assert rel(U.to_logical(), orc.bmul(-2.5 * ik[1] * specs[1])) <= tol
+
+
+def test_taylor_green_fused_divergence_and_curl(cuda):
+    """reference test/taylor_green.jl:125-150: zero divergence and the exact
+    vorticity, each from one fused backward transform."""
+    g = np.load(os.path.join(GOLD, "taylor_green_16_8_16.npz"))
+    dims = (16, 8, 16)
+    Ls = tuple(float(v) for v in g["L"])
+    plan = P.PencilFFTPlan(dims, T.RFFT(), np.float64)
+    u = plan.allocate_input(P.Val(3))
+    for c, x in zip(u, g["u"]):
+        c.copy_from_logical(x)
+    uF = plan * u
+    div = plan.allocate_input()
+    P.ldiv_divergence_(div, plan, uF, Ls)
+    assert np.max(np.abs(div.to_logical())) < 1e-12
+    om = plan.allocate_input(P.Val(3))
+    P.ldiv_curl_(om, plan, uF, Ls)
+    err = sum(np.sum((o.to_logical() - wr) ** 2) for o, wr in zip(om, g["w"]))
+    assert err < 1e-16 * 1e3  # reference test/taylor_green.jl:148-149
+
+
+def test_derivative_sum_errors(cuda):
+    plan = P.PencilFFTPlan((16, 12, 8), T.RFFT(), np.float64)
+    A = plan.allocate_input()
+    B = plan.allocate_output()
+    with pytest.raises(P.ArgumentError, match="1 to 3 terms"):
+        P.ldiv_deriv_sum_(A, plan, [(B, 1, 1.0, 1.0)] * 4)
+    with pytest.raises(P.ArgumentError):
+        P.ldiv_deriv_sum_(A, plan, [(B, 4, 1.0, 1.0)])
+    pip = P.PencilFFTPlan((16, 12, 8), T.FFT_(), np.float64)
+    M = pip.allocate_input()
+    with pytest.raises(P.ArgumentError):
+        P.ldiv_deriv_sum_(M, pip, [(M, 1, 1.0, 1.0)])
