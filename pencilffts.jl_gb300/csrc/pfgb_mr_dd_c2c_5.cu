@@ -1,0 +1,13 @@
+// Mixed-radix register pass (lines of 5 * 2^k points), double-float (dd) arithmetic for Float64 data, c2c lines.
+#include <cuda_runtime.h>
+
+#include "pencilfft_gb300.h"
+#include "pfgb_mr.cuh"
+
+namespace pfgb {
+
+int launch_mr_dd_c2c_5(int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_mr_r0<dd, 5, OP_C2C>(logn, sign, A, grid, s);
+}
+
+}  // namespace pfgb

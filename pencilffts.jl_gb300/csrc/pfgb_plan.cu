@@ -23,6 +23,7 @@
 #include "pencilfft_gb300.h"
 #include "pfgb_device.cuh"
 #include "pfgb_fast.cuh"
+#include "pfgb_mr.cuh"
 #include "pfgb_tc.cuh"
 
 namespace pfgb {
@@ -109,6 +110,10 @@ struct Pass {
   // RODFT00 through their power-of-two extensions)
   bool fast = false;
   int fop = -1;
+  // mixed-radix register pass (mr_pass) for lines of r0 * 2^logn points
+  bool mr = false;
+  int r0 = 0, logn = 0;
+  const void* ftw2 = nullptr;  // its r0 * 2^logn-point twiddle table
   // Float64 fast passes: dd-form input / output between consecutive dd passes,
   // and an exponent reduction over the input before the first pass of a run
   bool in_dd = false, out_dd = false, reduce_before = false;
@@ -573,6 +578,31 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
     }
     return PFGB_OK;
   }
+  // lines of 3 * 2^k and 5 * 2^k points (8 <= 2^k <= 512) take the
+  // mixed-radix register pass, in dd for Float64 data unless native FP64
+  // was requested
+  if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && ps.L == 0 &&
+      !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+    for (int r0 : {3, 5}) {
+      if (M % r0) continue;
+      const int n = M / r0;
+      if (n < 8 || n > 512 || (n & (n - 1))) continue;
+      ps.mr = true;
+      ps.fop = ps.op;
+      ps.r0 = r0;
+      ps.logn = 0;
+      while ((1 << ps.logn) < n) ++ps.logn;
+      rc = upload_fast_table(P, n, &ps.ftw);
+      if (!rc) rc = upload_fast_table(P, M, &ps.ftw2);
+      if (rc) return rc;
+      const bool packed = fast_packed(ps.op);
+      ps.clines = P->rb == 8 ? mr_tw<dd>(ps.logn) : mr_tw<float>(ps.logn);
+      ps.lines = packed ? 2 * ps.clines : ps.clines;
+      ps.threads = P->rb == 8 ? mr_threads<dd>(ps.logn) : mr_threads<float>(ps.logn);
+      ps.smem = P->rb == 8 ? mr_smem<dd>(r0, ps.logn, ps.op) : mr_smem<float>(r0, ps.logn, ps.op);
+      return PFGB_OK;
+    }
+  }
   const int Lc = ps.L > 0 ? ps.L : ps.M;
   int rmin = 64;
   for (int i = 0; i < ps.nst; ++i) rmin = std::min(rmin, ps.rad[i]);
@@ -780,6 +810,7 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.in = in;
   F.out = out;
   F.tw = ps.ftw;
+  F.tw2 = ps.ftw2;
   F.op = ps.fop;
   F.r2r_odd = ps.r2r_kind == K_RODFT00 ? 1 : 0;
   F.n_in = A.n_in;
@@ -895,6 +926,31 @@ int launch_fast_fx(int logm, int sign, const FastArgs& A, int64_t grid, cudaStre
 int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_tc(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_fast_tma_dd(int logm, int sign, const FastArgs& A, cudaStream_t s);
+int launch_mr_f32_c2c(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_mr_f32_r2c(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_mr_f32_c2r(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_mr_dd_c2c(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_mr_dd_r2c(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_mr_dd_c2r(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+
+// mixed-radix pass of a plan (grid == 0: configure only); OP_CSUM runs the
+// c2c kernel (its load sums the terms)
+static int launch_mr(const pfgb_plan* P, const Pass& ps, const FastArgs& F, int64_t grid, cudaStream_t s) {
+  const bool d = P->rb == 8;
+  switch (F.op) {
+    case OP_C2C: case OP_CSUM:
+      return d ? launch_mr_dd_c2c(ps.r0, ps.logn, ps.sign, F, grid, s)
+               : launch_mr_f32_c2c(ps.r0, ps.logn, ps.sign, F, grid, s);
+    case OP_R2C:
+      return d ? launch_mr_dd_r2c(ps.r0, ps.logn, ps.sign, F, grid, s)
+               : launch_mr_f32_r2c(ps.r0, ps.logn, ps.sign, F, grid, s);
+    case OP_C2R:
+      return d ? launch_mr_dd_c2r(ps.r0, ps.logn, ps.sign, F, grid, s)
+               : launch_mr_f32_c2r(ps.r0, ps.logn, ps.sign, F, grid, s);
+    default:
+      return fail(PFGB_ERR_UNSUPPORTED, "internal: mixed-radix pass operation");
+  }
+}
 
 #ifndef PFGB_FAST_TMA
 #define PFGB_FAST_TMA 0
@@ -1214,6 +1270,13 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
                         : launch_fast_f32(ps.logm, ps.sign, F, grid, s);
       }
       if (rc) return rc;
+    } else if (ps.mr) {
+      FastArgs F;
+      int64_t grid = 0;
+      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr);
+      if (rc) return rc;
+      rc = launch_mr(P, ps, F, grid, s);
+      if (rc) return rc;
     } else {
       PassArgs A;
       int64_t grid = 0;
@@ -1419,6 +1482,11 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
             rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
                             : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);
           if (!rc && ps.tc) rc = launch_tc(ps.logm, ps.sign, F, nullptr);
+        } else if (ps.mr) {
+          FastArgs F;
+          std::memset(&F, 0, sizeof(F));
+          F.op = ps.fop;
+          rc = launch_mr(P, ps, F, 0, nullptr);
         } else {
           PassArgs A;
           std::memset(&A, 0, sizeof(A));
@@ -1592,6 +1660,7 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
                         : ps.tc ? "tc_pass<tf32x3>"
                         : ps.variant == 1 ? (P->rb == 8 ? "fast_pass_tma<dd>" : "fast_pass_tma<float>")
                         : ps.fast ? (P->rb == 4 ? "fast_pass<float>" : P->fx ? "fast_pass<fx>" : "fast_pass<dd>")
+                        : ps.mr ? (P->rb == 4 ? "mr_pass<float>" : "mr_pass<dd>")
                                   : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);
     acc.push_back(e);
