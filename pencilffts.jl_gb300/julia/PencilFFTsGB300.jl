@@ -6,9 +6,21 @@ PencilFFTs.jl at `proc_dims = (1, ..., 1)` on one GB300 GPU.
 
 `GB300Plan(dims, transforms, real_type; permute_dims, extra_dims, fftw_flags,
 precision)` is the device counterpart of `PencilFFTPlan(dims, transforms,
-proc_dims, comm, real_type; ...)` (reference src/plans.jl:306-320); `mul!`, `ldiv!` and `bmul!` take `CuArray`s
-laid out as the reference's `PencilArray` parents: input in natural order,
-output with its dimensions reversed when `permute_dims = Val(true)`.
+proc_dims, comm, real_type; ...)` (reference src/plans.jl:306-320).  The
+reference's user API is mirrored on `CuArray`s laid out as the reference's
+`PencilArray` parents (input in natural order, output with its dimensions
+reversed when `permute_dims = Val(true)`):
+
+- `mul!`, `ldiv!`, `bmul!` (src/operations.jl:24-52), also over tuples and
+  arrays of arrays (src/operations.jl:129-152);
+- `p * u` and `p \ uF` (src/operations.jl:54-62);
+- `allocate_input(p)`, `allocate_output(p)` and their `Val(N)` / dims forms
+  (src/allocate.jl:44-122); in-place plans return one buffer holding the
+  input and output views (`ManyCuArray`, the counterpart of
+  `ManyPencilArray`);
+- `scale_factor`, `size`, `is_inplace`, `eltype_input`, `eltype_output`;
+- the fused spectral operators of the library: `ldiv_deriv!` (one i k
+  multiply), `ldiv_divergence!` and `ldiv_curl!` (test/include/FourierOperations.jl).
 
 The transforms are the reference's own `Transforms` types; the mapping to the
 C ABI codes is `abi_kind`.
@@ -40,6 +52,26 @@ struct PlanDesc
     extra_dims::NTuple{MAX_EXTRA,Int64}
     precision_mode::Int32
     autotune::Int32
+end
+
+# pfgb_plan_info (include/pencilfft_gb300.h); Julia lays out isbits structs
+# with C alignment, so the field order and types are the whole contract
+struct PlanInfo
+    ndims::Int32
+    dims_in::NTuple{MAX_DIMS,Int64}
+    dims_out::NTuple{MAX_DIMS,Int64}
+    perm_out::NTuple{MAX_DIMS,Int32}
+    eltype_in_complex::Int32
+    eltype_out_complex::Int32
+    real_bytes::Int32
+    inplace::Int32
+    scale_factor::Float64
+    input_bytes::Int64
+    output_bytes::Int64
+    inplace_bytes::Int64
+    scratch_bytes::Int64
+    n_passes_forward::Int32
+    n_passes_backward::Int32
 end
 
 # PFGB_PRECISION_* (include/pencilfft_gb300.h): :default (Float64 power-of-two
@@ -77,6 +109,8 @@ mutable struct GB300Plan{T,N}
     handle::Ptr{Cvoid}
     transforms::NTuple{N,Transforms.AbstractTransform}
     scale::Float64
+    info::PlanInfo
+    extra_dims::Dims
     function GB300Plan(dims::Dims{N}, transforms, ::Type{T} = Float64;
                        permute_dims::Val{P} = Val(true), extra_dims::Dims = (),
                        fftw_flags = FFTW.ESTIMATE, precision::Symbol = :default) where {N,T,P}
@@ -94,10 +128,9 @@ mutable struct GB300Plan{T,N}
                         autotune_code(fftw_flags))
         h = Ref{Ptr{Cvoid}}(C_NULL)
         check(ccall((:pfgb_plan_create, LIB), Cint, (Ref{PlanDesc}, Ref{Ptr{Cvoid}}), desc, h))
-        info = Vector{UInt8}(undef, 512)
-        check(ccall((:pfgb_plan_info_get, LIB), Cint, (Ptr{Cvoid}, Ptr{UInt8}), h[], info))
-        scale = unsafe_load(Ptr{Float64}(pointer(info) + 184))  # pfgb_plan_info.scale_factor (byte offset 184)
-        p = new{T,N}(h[], trs, scale)
+        info = Ref{PlanInfo}()
+        check(ccall((:pfgb_plan_info_get, LIB), Cint, (Ptr{Cvoid}, Ref{PlanInfo}), h[], info))
+        p = new{T,N}(h[], trs, info[].scale_factor, info[], extra_dims)
         finalizer(p) do q
             ccall((:pfgb_plan_destroy, LIB), Cint, (Ptr{Cvoid},), q.handle)
         end
@@ -106,10 +139,71 @@ mutable struct GB300Plan{T,N}
 end
 
 scale_factor(p::GB300Plan) = p.scale
+is_inplace(p::GB300Plan) = p.info.inplace != 0
+Base.size(p::GB300Plan{T,N}) where {T,N} = ntuple(i -> Int(p.info.dims_in[i]), Val(N))
+size_out(p::GB300Plan{T,N}) where {T,N} = ntuple(i -> Int(p.info.dims_out[i]), Val(N))
+eltype_input(p::GB300Plan{T}) where {T} = p.info.eltype_in_complex != 0 ? Complex{T} : T
+eltype_output(p::GB300Plan{T}) where {T} = p.info.eltype_out_complex != 0 ? Complex{T} : T
+
+# memory shapes of the input (natural order) and output (perm_out: fastest
+# logical dimension first) arrays, extra dimensions last
+input_shape(p::GB300Plan) = (size(p)..., p.extra_dims...)
+function output_shape(p::GB300Plan{T,N}) where {T,N}
+    (ntuple(i -> Int(p.info.dims_out[p.info.perm_out[i] + 1]), Val(N))..., p.extra_dims...)
+end
+
+# In-place plans: one buffer holding the input and output views (the
+# counterpart of ManyPencilArray, reference src/multiarrays_r2c.jl)
+struct ManyCuArray{Tb}
+    buffer::Tb
+    input::CuArray
+    output::CuArray
+end
+
+function _alloc(p::GB300Plan, which::Symbol)
+    if is_inplace(p)
+        buf = CuArray{UInt8}(undef, Int(p.info.inplace_bytes))
+        ti, to = eltype_input(p), eltype_output(p)
+        ishape = input_shape(p)
+        if ti <: Real && to <: Complex  # RFFT!: real view padded to 2 (n1/2 + 1)
+            ishape = (2 * (ishape[1] ÷ 2 + 1), Base.tail(ishape)...)
+        end
+        vin = reshape(reinterpret(ti, view(buf, 1:(prod(ishape) * sizeof(ti)))), ishape)
+        vout = reshape(reinterpret(to, view(buf, 1:(prod(output_shape(p)) * sizeof(to)))), output_shape(p))
+        return ManyCuArray(buf, vin, vout)
+    end
+    which === :in ? CuArray{eltype_input(p)}(undef, input_shape(p)) :
+                    CuArray{eltype_output(p)}(undef, output_shape(p))
+end
+
+# reference src/allocate.jl:44-122
+allocate_input(p::GB300Plan) = _alloc(p, :in)
+allocate_output(p::GB300Plan) = _alloc(p, :out)
+allocate_input(p::GB300Plan, ::Val{M}) where {M} = ntuple(_ -> allocate_input(p), Val(M))
+allocate_output(p::GB300Plan, ::Val{M}) where {M} = ntuple(_ -> allocate_output(p), Val(M))
+allocate_input(p::GB300Plan, dims...) = [allocate_input(p) for _ in CartesianIndices(dims)]
+allocate_output(p::GB300Plan, dims...) = [allocate_output(p) for _ in CartesianIndices(dims)]
 
 stream_ptr() = Ptr{Cvoid}(UInt(cuda_stream().handle))
 
+_ptr(A::ManyCuArray) = pointer(A.buffer)
+_ptr(A::CuArray) = pointer(A)
+
 # reference src/operations.jl:24-31
+function LinearAlgebra.mul!(dst::ManyCuArray, p::GB300Plan, src::ManyCuArray)
+    dst === src || throw(ArgumentError("input and output arrays for in-place plan must be the same"))
+    check(ccall((:pfgb_forward, LIB), Cint, (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}),
+                p.handle, _ptr(dst), _ptr(src), stream_ptr()))
+    dst
+end
+function LinearAlgebra.ldiv!(dst::ManyCuArray, p::GB300Plan, src::ManyCuArray)
+    dst === src || throw(ArgumentError("input and output arrays for in-place plan must be the same"))
+    check(ccall((:pfgb_backward, LIB), Cint,
+                (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}, Cint),
+                p.handle, _ptr(dst), _ptr(src), stream_ptr(), 1))
+    dst
+end
+
 function LinearAlgebra.mul!(dst::CuArray, p::GB300Plan, src::CuArray)
     check(ccall((:pfgb_forward, LIB), Cint, (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}),
                 p.handle, dst, src, stream_ptr()))
@@ -130,6 +224,66 @@ function bmul!(dst::CuArray, p::GB300Plan, src::CuArray)
                 (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}, Cint),
                 p.handle, dst, src, stream_ptr(), 0))
     dst
+end
+
+# reference src/operations.jl:54-62: allocating forms
+Base.:*(p::GB300Plan, src::CuArray) = mul!(allocate_output(p), p, src)
+Base.:\(p::GB300Plan, src::CuArray) = ldiv!(allocate_input(p), p, src)
+Base.:*(p::GB300Plan, A::ManyCuArray) = mul!(A, p, A)
+Base.:\(p::GB300Plan, A::ManyCuArray) = ldiv!(A, p, A)
+
+# reference src/operations.jl:129-152: collections of fields
+const Collection = Union{Tuple{Vararg{Union{CuArray,ManyCuArray}}},AbstractArray{<:Union{CuArray,ManyCuArray}}}
+function _check_lengths(dst, src)
+    length(dst) == length(src) || throw(ArgumentError("collections have different lengths"))
+end
+for f in (:mul!, :ldiv!)
+    @eval function LinearAlgebra.$f(dst::Collection, p::GB300Plan, src::Collection)
+        _check_lengths(dst, src)
+        foreach((d, s) -> $f(d, p, s), dst, src)
+        dst
+    end
+end
+function bmul!(dst::Collection, p::GB300Plan, src::Collection)
+    _check_lengths(dst, src)
+    foreach((d, s) -> bmul!(d, p, s), dst, src)
+    dst
+end
+Base.:*(p::GB300Plan, src::Collection) = map(s -> p * s, src)
+Base.:\(p::GB300Plan, src::Collection) = map(s -> p \ s, src)
+
+# Spectral operators fused into the first backward pass (no counterpart in
+# the reference API: the reference multiplies by i k in Fourier space, then
+# calls ldiv!; examples/gradient.jl, test/include/FourierOperations.jl).
+# dims are 1-based, L the domain lengths.
+function ldiv_deriv!(dst::CuArray, p::GB300Plan, src::CuArray, dim::Integer, L::Real)
+    check(ccall((:pfgb_backward_deriv, LIB), Cint,
+                (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cdouble),
+                p.handle, dst, src, stream_ptr(), 1, dim - 1, L))
+    dst
+end
+function _deriv_sum!(dst::CuArray, p::GB300Plan, terms)
+    n = length(terms)
+    srcs = Ptr{Cvoid}[Ptr{Cvoid}(UInt(pointer(t[1]))) for t in terms]
+    dims = Cint[t[2] - 1 for t in terms]
+    coefs = Cdouble[t[3] for t in terms]
+    lens = Cdouble[t[4] for t in terms]
+    check(ccall((:pfgb_backward_deriv_sum, LIB), Cint,
+                (Ptr{Cvoid}, CuPtr{Cvoid}, Ptr{Ptr{Cvoid}}, Cint, Ptr{Cint}, Ptr{Cdouble}, Ptr{Cdouble},
+                 Ptr{Cvoid}, Cint),
+                p.handle, dst, srcs, n, dims, coefs, lens, stream_ptr(), 1))
+    dst
+end
+# ∇⋅u from the spectra uF (one per dimension)
+ldiv_divergence!(dst::CuArray, p::GB300Plan, uF, L) =
+    _deriv_sum!(dst, p, [(uF[d], d, 1.0, L[d]) for d in eachindex(uF)])
+# ∇×u in 3D, one fused backward transform per component
+function ldiv_curl!(ω, p::GB300Plan{T,3}, uF, L) where {T}
+    for a in 1:3
+        b, c = mod1(a + 1, 3), mod1(a + 2, 3)
+        _deriv_sum!(ω[a], p, [(uF[c], b, 1.0, L[b]), (uF[b], c, -1.0, L[c])])
+    end
+    ω
 end
 
 end # module

@@ -50,3 +50,32 @@ def test_null_arguments_rejected_without_device():
     assert L.pfgb_plan_create(None, None) == _lib.ERR_ARGUMENT
     assert L.pfgb_forward(None, None, None, None) == _lib.ERR_ARGUMENT
     assert L.pfgb_plan_destroy(None) == _lib.OK
+
+
+def _julia_struct(name):
+    """Fields (name, ctypes type) of an isbits struct of the Julia binding."""
+    src = open(os.path.join(REPO, "pencilffts.jl_gb300", "julia", "PencilFFTsGB300.jl")).read()
+    m = re.search(r"^struct %s\n(.*?)^end" % name, src, flags=re.S | re.M)
+    assert m, name
+    scalar = {"Int32": ctypes.c_int32, "Int64": ctypes.c_int64, "Float64": ctypes.c_double}
+    consts = {"MAX_DIMS": _lib.MAX_DIMS, "MAX_EXTRA": 4}
+    out = []
+    for line in m.group(1).strip().splitlines():
+        fname, ftype = [t.strip() for t in line.split("::")]
+        t = re.fullmatch(r"NTuple\{(\w+),(\w+)\}", ftype)
+        out.append((fname, scalar[t.group(2)] * consts[t.group(1)] if t else scalar[ftype]))
+    return out
+
+
+def test_julia_structs_mirror_the_header():
+    """The Julia binding's PlanDesc and PlanInfo have the C structs' fields, in
+    order and with the same types (Julia lays isbits structs out with C
+    alignment), so ccall passes them by reference unchanged."""
+    for jname, cstruct in (("PlanDesc", _lib.PlanDesc), ("PlanInfo", _lib.PlanInfo)):
+        jf = _julia_struct(jname)
+        cf = cstruct._fields_
+        assert [n for n, _ in jf] == [n for n, _ in cf], jname
+        for (n, jt), (_, ct) in zip(jf, cf):
+            assert ctypes.sizeof(jt) == ctypes.sizeof(ct) and getattr(jt, "_type_", jt) == getattr(ct, "_type_", ct), (jname, n)
+    # offsets the binding relies on, e.g. scale_factor of pfgb_plan_info
+    assert _lib.PlanInfo.scale_factor.offset == 184
