@@ -728,8 +728,10 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     }
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
-  } else {  // OP_C2R: Hermitian extension of two half spectra, n = M, m = n_in
-    const int m = a.n_in;
+  } else {  // OP_C2R: Hermitian extension of two half spectra, n = M
+    // m = n_in = M/2 + 1 (power-of-two M): the extension's case distinctions
+    // are compile-time for every register but r = 0 and r = 4
+    constexpr int m = M / 2 + 1;
     const int i0 = 2 * p, i1 = 2 * p + 1;
     MC ra[8], rb[8];
     if (!(IO::kDD && IN_DD)) {
@@ -900,7 +902,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     }
   } else if constexpr (OP == OP_R2C) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
-    const int m = a.n_out;
+    constexpr int m = M / 2 + 1;  // n_out of a power-of-two r2c line
     const int tot = TW * m;
     for (int e = tid; e < tot; e += nth) {
       int q, k;
@@ -908,8 +910,12 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       const Cx<R> f = z[sidx<R, LOGM, OP>(q, k)];
       const Cx<R> g = conj(z[sidx<R, LOGM, OP>(q, k == 0 ? 0 : M - k)]);
       Cx<R> A = f + g, B = mul_mi(f - g);
-      A = apply_scale(mk(half(A.re), half(A.im)), a);
-      B = apply_scale(mk(half(B.re), half(B.im)), a);
+      if constexpr (!IO::kDD) {
+        A = mk(half(A.re), half(A.im));
+        B = mk(half(B.re), half(B.im));
+      }  // dd: the factor 1/2 is one less in the run's output exponent (emax_shift)
+      A = apply_scale(A, a);
+      B = apply_scale(B, a);
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const int64_t off = (int64_t)k * a.out_sa;
       if (IO::kDD && OUT_DD) {
@@ -1082,7 +1088,7 @@ __device__ __forceinline__ void fast_tile_fx(const FastArgs& a, int64_t bid, Cx<
     // exponents first (input lines' words, or the doubles' exponents), then
     // load, convert and combine after the line's scale is known (the second
     // reads hit L1); holding the raw values across the barrier would spill
-    const int m = a.n_in;
+    constexpr int m = M / 2 + 1;
     const int i0 = 2 * p, i1 = 2 * p + 1;
     int tm = kTeZero;
     unsigned emx = 0;
@@ -1230,7 +1236,7 @@ __device__ __forceinline__ void fast_tile_fx(const FastArgs& a, int64_t bid, Cx<
       }
     }
   } else if constexpr (OP == OP_R2C) {
-    const int m = a.n_out;
+    constexpr int m = M / 2 + 1;
     const int tot = TW * m;
     for (int e = tid; e < tot; e += nth) {
       int q, k;

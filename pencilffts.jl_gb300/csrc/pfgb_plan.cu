@@ -121,6 +121,10 @@ struct Pass {
   // each tile by itself (self_scale); the second maps each element to its
   // first-pass tile (te_rescale, te_sh / te_mul per role)
   bool self_scale = false, te_rescale = false;
+  // the last pass of a double-float run that starts with an r2c pass: the
+  // r2c split leaves out its factor 1/2, which this pass's output exponent
+  // takes instead
+  bool half_fold = false;
   int te_sh[2 + kMaxOuter] = {};
   unsigned te_mul[2 + kMaxOuter] = {};
   int logm = 0;
@@ -853,6 +857,7 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
       F.emax_shift = k;
     }
   }
+  if (ps.half_fold && fxi < 0) F.emax_shift -= 1;
   if (fxi >= 0) {
     F.tw = ps.ftw_fx;
     F.te_in = ps.in_dd ? P->te_fx[(fxi + 1) & 1] : nullptr;
@@ -1449,6 +1454,14 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
         v[i].out_dd = next;
         v[i].reduce_before = !prev;
         v[i].self_scale = !prev;
+      }
+      // runs that start with an r2c pass: its split's factor 1/2 goes into
+      // the output exponent of the run's last pass
+      for (size_t i = 0; i < v.size(); ++i) {
+        if (!v[i].fast || v[i].fop != OP_R2C || v[i].in_dd) continue;
+        size_t j = i;
+        while (v[j].out_dd) ++j;
+        v[j].half_fold = true;
       }
       // element -> previous-pass line maps: the second pass of a dd run
       // (te_rescale) and every pass of an fx run with fx input

@@ -157,6 +157,12 @@ class GPULocalTransforms:
     def __call__(self, x, axis: int, tr, n_out: int):
         from .plans import PencilArray, PencilFFTPlan, mul_
         torch = _torch()
+        if x.is_complex() and isinstance(tr, Tr.R2R):
+            # an R2R stage on complex data (after an FFT stage): the real and
+            # imaginary parts as one real block with a trailing dimension of 2
+            # (a plan of R2R and NoTransform alone takes real input)
+            y = self(torch.view_as_real(x.contiguous()), axis, tr, n_out)
+            return torch.view_as_complex(y.contiguous())
         N = x.dim()
         # a C-ordered logical block is the column-major array of the
         # reversed dimensions: transform dimension N - 1 - axis of that plan
