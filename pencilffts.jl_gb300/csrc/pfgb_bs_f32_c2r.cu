@@ -1,0 +1,13 @@
+// Bluestein register pass (lines of any length up to 2048), Float32 arithmetic, c2r lines.
+#include <cuda_runtime.h>
+
+#include "pencilfft_gb300.h"
+#include "pfgb_bs.cuh"
+
+namespace pfgb {
+
+int launch_bs_f32_c2r(int logl, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_bs_op<float, OP_C2R>(logl, A, grid, s);
+}
+
+}  // namespace pfgb

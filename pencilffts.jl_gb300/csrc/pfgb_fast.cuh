@@ -32,6 +32,12 @@ struct FastArgs {
   void* out;
   const void* tw;  // M entries exp(-2 pi i m / M) as Cx<R>
   const void* tw2; // mixed-radix pass (mr_pass): R0 N entries exp(-2 pi i m / (R0 N)); tw has N
+  // Bluestein pass (bs_pass): DFT length, chirp w[j] (bs_m entries), filter
+  // spectrum (L entries, 1/L included), divisor of its store loop
+  int bs_m;
+  const void* bs_chirp;
+  const void* bs_filt;
+  Div31 div_m;
   int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R
   int r2r_odd;     // OP_X00C / OP_X00R: 0 REDFT00 (even extension), 1 RODFT00 (odd)
   int n_in, n_out;

@@ -24,6 +24,7 @@
 #include "pfgb_device.cuh"
 #include "pfgb_fast.cuh"
 #include "pfgb_mr.cuh"
+#include "pfgb_bs.cuh"
 #include "pfgb_tc.cuh"
 
 namespace pfgb {
@@ -114,6 +115,16 @@ struct Pass {
   bool mr = false;
   int r0 = 0, logn = 0;
   const void* ftw2 = nullptr;  // its r0 * 2^logn-point twiddle table
+  // Bluestein register pass (bs_pass) for other lines up to 2048 points:
+  // convolution length 2^logl (ftw holds its twiddles), chirp and filter
+  // tables; the generic kernel's geometry is kept (g_*) for executions it
+  // must take (a fused derivative on this pass)
+  bool bs = false;
+  int logl = 0;
+  const void* bs_chirp = nullptr;
+  const void* bs_filt = nullptr;
+  int g_lines = 0, g_clines = 0, g_threads = 0;
+  size_t g_smem = 0;
   // Float64 fast passes: dd-form input / output between consecutive dd passes,
   // and an exponent reduction over the input before the first pass of a run
   bool in_dd = false, out_dd = false, reduce_before = false;
@@ -346,6 +357,60 @@ static int upload_fast_table(pfgb_plan* P, int M, const void** out) {
   P->tables[key] = d;
   *out = d;
   return PFGB_OK;
+}
+
+// A complex table in the register kernels' format (float (re, im), or dd
+// (re.hi, re.lo, im.hi, im.lo) for Float64 plans).
+static int upload_fast_vec(pfgb_plan* P, const std::string& key, const std::vector<std::complex<ld>>& v,
+                           const void** out) {
+  if (P->query_only) {
+    *out = nullptr;
+    return PFGB_OK;
+  }
+  const std::string k = (P->rb == 8 ? "fvdd" : "fvf") + key;
+  auto it = P->tables.find(k);
+  if (it != P->tables.end()) {
+    *out = it->second;
+    return PFGB_OK;
+  }
+  std::vector<float> h;
+  h.reserve(v.size() * 4);
+  for (const auto& w : v) {
+    if (P->rb == 8) {
+      for (ld c : {w.real(), w.imag()}) {
+        const float hi = (float)c;
+        h.push_back(hi);
+        h.push_back((float)(c - (ld)hi));
+      }
+    } else {
+      h.push_back((float)w.real());
+      h.push_back((float)w.imag());
+    }
+  }
+  void* d = nullptr;
+  PFGB_CUDA(cudaMalloc(&d, std::max<size_t>(h.size() * sizeof(float), 16)));
+  PFGB_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  P->tables[k] = d;
+  *out = d;
+  return PFGB_OK;
+}
+
+// Bluestein tables of a length-M DFT of sign `sign` with convolution length
+// L >= 2M - 1: chirp w[j] = exp(sign i pi j^2 / M) (j < M) and the filter
+// spectrum FFT_L(b) / L of b[j] = conj(w[j]), b[L - j] = conj(w[j]).
+static void bluestein_tables(int M, int L, int sign, std::vector<std::complex<ld>>& w,
+                             std::vector<std::complex<ld>>& bf) {
+  w.assign(M, {0, 0});
+  for (int j = 0; j < M; ++j) {
+    const int64_t jj = ((int64_t)j * j) % (2 * (int64_t)M);
+    w[j] = expi_pi(jj, M);  // exp(-i pi j^2 / M)
+    if (sign > 0) w[j] = std::conj(w[j]);
+  }
+  bf.assign(L, {0, 0});
+  for (int j = 0; j < M; ++j) bf[j] = std::conj(w[j]);
+  for (int j = 1; j < M; ++j) bf[L - j] = std::conj(w[j]);
+  host_fft_pow2(bf, -1);
+  for (auto& x : bf) x /= (ld)L;
 }
 
 // Twiddles of the fast kernel in fx form: exp(sign 2 pi i m / M) as
@@ -633,6 +698,32 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   if (ps.smem > 200 * 1024)
     return fail(PFGB_ERR_UNSUPPORTED, "line does not fit in shared memory");
   ps.zero_fill = ps.L > 0 || (ps.op == OP_R2R_C || ps.op == OP_R2R_R);
+  // other c2c / r2c / c2r lines up to 2048 points take the Bluestein register
+  // pass (double-float for Float64 data unless native FP64 was requested)
+  if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && M >= 2 && M <= 2048 &&
+      !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+    int logl = 4;
+    while ((1 << logl) < 2 * M - 1) ++logl;
+    std::vector<std::complex<ld>> w, bf;
+    bluestein_tables(M, 1 << logl, ps.sign, w, bf);
+    const std::string key = std::to_string(M) + "/" + std::to_string(1 << logl) + (ps.sign > 0 ? "+" : "-");
+    int rc2 = upload_fast_table(P, 1 << logl, &ps.ftw);
+    if (!rc2) rc2 = upload_fast_vec(P, "bsw" + key, w, &ps.bs_chirp);
+    if (!rc2) rc2 = upload_fast_vec(P, "bsf" + key, bf, &ps.bs_filt);
+    if (rc2) return rc2;
+    ps.g_lines = ps.lines;
+    ps.g_clines = ps.clines;
+    ps.g_threads = ps.threads;
+    ps.g_smem = ps.smem;
+    ps.bs = true;
+    ps.fop = ps.op;
+    ps.logl = logl;
+    const bool pk = fast_packed(ps.op);
+    ps.clines = P->rb == 8 ? bs_tw<dd>(logl) : bs_tw<float>(logl);
+    ps.lines = pk ? 2 * ps.clines : ps.clines;
+    ps.threads = P->rb == 8 ? bs_threads<dd>(logl) : bs_threads<float>(logl);
+    ps.smem = P->rb == 8 ? bs_smem<dd>(logl) : bs_smem<float>(logl);
+  }
   return PFGB_OK;
 }
 
@@ -937,6 +1028,35 @@ int launch_mr_f32_c2r(int r0, int logn, int sign, const FastArgs& A, int64_t gri
 int launch_mr_dd_c2c(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_mr_dd_r2c(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_mr_dd_c2r(int r0, int logn, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+
+int launch_bs_f32_c2c(int logl, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_bs_f32_r2c(int logl, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_bs_f32_c2r(int logl, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_bs_dd_c2c(int logl, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_bs_dd_r2c(int logl, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_bs_dd_c2r(int logl, const FastArgs& A, int64_t grid, cudaStream_t s);
+
+// Bluestein pass of a plan (grid == 0: configure only)
+static int launch_bs(const pfgb_plan* P, const Pass& ps, const FastArgs& F, int64_t grid, cudaStream_t s) {
+  const bool d = P->rb == 8;
+  switch (ps.op) {
+    case OP_C2C: return d ? launch_bs_dd_c2c(ps.logl, F, grid, s) : launch_bs_f32_c2c(ps.logl, F, grid, s);
+    case OP_R2C: return d ? launch_bs_dd_r2c(ps.logl, F, grid, s) : launch_bs_f32_r2c(ps.logl, F, grid, s);
+    case OP_C2R: return d ? launch_bs_dd_c2r(ps.logl, F, grid, s) : launch_bs_f32_c2r(ps.logl, F, grid, s);
+    default: return fail(PFGB_ERR_UNSUPPORTED, "internal: Bluestein pass operation");
+  }
+}
+
+// The generic-kernel form of a Bluestein pass (its own geometry)
+static Pass generic_form(const Pass& ps) {
+  Pass g = ps;
+  g.bs = false;
+  g.lines = ps.g_lines;
+  g.clines = ps.g_clines;
+  g.threads = ps.g_threads;
+  g.smem = ps.g_smem;
+  return g;
+}
 
 // mixed-radix pass of a plan (grid == 0: configure only); OP_CSUM runs the
 // c2c kernel (its load sums the terms)
@@ -1282,12 +1402,27 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       if (rc) return rc;
       rc = launch_mr(P, ps, F, grid, s);
       if (rc) return rc;
+    } else if (ps.bs && ps.variant != 2 && !(i == dpass && dv && dv->mode)) {
+      FastArgs F;
+      int64_t grid = 0;
+      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, nullptr);
+      if (rc) return rc;
+      F.bs_m = ps.M;
+      F.bs_chirp = ps.bs_chirp;
+      F.bs_filt = ps.bs_filt;
+      F.div_m = make_div31(ps.op == OP_R2C ? ps.M / 2 + 1 : ps.M);
+      rc = launch_bs(P, ps, F, grid, s);
+      if (rc) return rc;
     } else {
+      // generic kernel (a Bluestein-eligible pass runs here with its generic
+      // geometry when a fused derivative applies to it, or when the planner
+      // measured this form faster)
+      const Pass g = ps.bs ? generic_form(ps) : ps;
       PassArgs A;
       int64_t grid = 0;
-      int rc = make_args(P, ps, in, out, normalise && i == last_tr, A, grid, i == dpass ? dv : nullptr);
+      int rc = make_args(P, g, in, out, normalise && i == last_tr, A, grid, i == dpass ? dv : nullptr);
       if (rc) return rc;
-      rc = launch_pass(P->rb, A, grid, ps.threads, ps.smem, s);
+      rc = launch_pass(P->rb, A, grid, g.threads, g.smem, s);
       if (rc) return rc;
     }
     if (P->timing) {
@@ -1500,6 +1635,15 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
           std::memset(&F, 0, sizeof(F));
           F.op = ps.fop;
           rc = launch_mr(P, ps, F, 0, nullptr);
+        } else if (ps.bs) {
+          FastArgs F;
+          std::memset(&F, 0, sizeof(F));
+          rc = launch_bs(P, ps, F, 0, nullptr);
+          if (!rc) {
+            PassArgs A;
+            std::memset(&A, 0, sizeof(A));
+            rc = launch_pass(P->rb, A, 0, 0, 0, nullptr);
+          }
         } else {
           PassArgs A;
           std::memset(&A, 0, sizeof(A));
@@ -1577,7 +1721,9 @@ int pfgb_plan_set_timing(pfgb_plan* P, int on) {
 // buffers filled with normal numbers (bytes 0x3F), and the faster is kept.
 // Alternatives today: c2r passes of Float32 and double-float plans, plain
 // fast_pass or the TMA-fed persistent form (when the buffers satisfy its
-// alignment).
+// alignment); lines taken by the Bluestein register pass, that pass or the
+// generic kernel (radix 2..16 stages in shared memory, or its own Bluestein
+// for long lines).
 static int autotune_passes(pfgb_plan* P) {
   const int e1023 = 1023;
   for (auto* dir : {&P->fwd, &P->bwd}) {
@@ -1622,6 +1768,59 @@ static int autotune_passes(pfgb_plan* P) {
         }
       }
       ps.variant = best[1] < best[0] ? 1 : 0;
+      if (ea) cudaEventDestroy(ea);
+      if (eb) cudaEventDestroy(eb);
+      cudaFree(bin);
+      cudaFree(bout);
+      if (rc) return rc;
+    }
+  }
+  // Bluestein-eligible passes: the Bluestein register pass (variant -1)
+  // against the generic kernel (variant 2) on the same buffers
+  for (auto* dir : {&P->fwd, &P->bwd}) {
+    for (auto& ps : dir->passes) {
+      if (!ps.bs) continue;
+      void* bin = nullptr;
+      void* bout = nullptr;
+      const size_t nin = (size_t)ps.lin.bytes(), nout = (size_t)ps.lout.bytes();
+      PFGB_CUDA(cudaMalloc(&bin, nin));
+      cudaError_t e = cudaMalloc(&bout, nout);
+      if (e != cudaSuccess) {
+        cudaFree(bin);
+        return fail(PFGB_ERR_ALLOC, std::string("cudaMalloc (autotune): ") + cudaGetErrorString(e));
+      }
+      cudaEvent_t ea = nullptr, eb = nullptr;
+      int rc = PFGB_OK;
+      float best[2] = {3.0e38f, 3.0e38f};
+      if ((e = cudaMemset(bin, 0x3F, nin)) != cudaSuccess || (e = cudaEventCreate(&ea)) != cudaSuccess ||
+          (e = cudaEventCreate(&eb)) != cudaSuccess)
+        rc = fail_cuda(e, "autotune set-up");
+      for (int v = 0; v < 2 && !rc; ++v) {
+        for (int it = 0; it < 7 && !rc; ++it) {
+          int64_t grid = 0;
+          cudaEventRecord(ea, 0);
+          if (v == 0) {
+            FastArgs F;
+            rc = make_fast_args(P, ps, bin, bout, false, F, grid);
+            F.bs_m = ps.M;
+            F.bs_chirp = ps.bs_chirp;
+            F.bs_filt = ps.bs_filt;
+            F.div_m = make_div31(ps.op == OP_R2C ? ps.M / 2 + 1 : ps.M);
+            if (!rc) rc = launch_bs(P, ps, F, grid, 0);
+          } else {
+            const Pass g = generic_form(ps);
+            PassArgs A;
+            rc = make_args(P, g, bin, bout, false, A, grid);
+            if (!rc) rc = launch_pass(P->rb, A, grid, g.threads, g.smem, 0);
+          }
+          cudaEventRecord(eb, 0);
+          if ((e = cudaEventSynchronize(eb)) != cudaSuccess) rc = fail_cuda(e, "autotune launch");
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, ea, eb);
+          if (it >= 2 && ms < best[v]) best[v] = ms;
+        }
+      }
+      ps.variant = best[1] < best[0] ? 2 : -1;
       if (ea) cudaEventDestroy(ea);
       if (eb) cudaEventDestroy(eb);
       cudaFree(bin);
@@ -1674,6 +1873,7 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
                         : ps.variant == 1 ? (P->rb == 8 ? "fast_pass_tma<dd>" : "fast_pass_tma<float>")
                         : ps.fast ? (P->rb == 4 ? "fast_pass<float>" : P->fx ? "fast_pass<fx>" : "fast_pass<dd>")
                         : ps.mr ? (P->rb == 4 ? "mr_pass<float>" : "mr_pass<dd>")
+                        : ps.bs && ps.variant != 2 ? (P->rb == 4 ? "bs_pass<float>" : "bs_pass<dd>")
                                   : (P->rb == 8 ? "pass_kernel<double>" : "pass_kernel<float>");
     std::snprintf(e.kernel, sizeof(e.kernel), "%s", kname);
     acc.push_back(e);
