@@ -84,10 +84,14 @@ typedef struct pfgb_plan_desc {
 } pfgb_plan_desc;
 
 /* Arithmetic of the transform kernels.
- *   DEFAULT:  Float32 plans compute in FP32; Float64 plans compute power-of-two
- *             c2c/r2c/c2r lines in double-float (two FP32 values, 48-bit
- *             significand, on the FP32 pipes) and every other line in native
- *             FP64.  Both meet a relative L2 error of 1e-13.
+ *   DEFAULT:  Float32 plans compute in FP32; Float64 plans compute in
+ *             double-float (two FP32 values, 48-bit significand, on the FP32
+ *             pipes) the c2c / r2c / c2r lines of up to 4096 points (power of
+ *             two), 3 * 2^k and 5 * 2^k points, and any other length up to
+ *             2048 (Bluestein), and REDFT00 / RODFT00 lines of 2^k +- 1
+ *             points; the remaining lines (other R2R kinds and lengths,
+ *             longer lines) in native FP64.  Both meet a relative L2 error of
+ *             1e-13.
  *   NATIVE:   Float64 plans compute every line in native FP64 (GB300's FP64
  *             rate is about 1/70 of its FP32 rate).
  *   TC_SPLIT: Float32 plans only: c2c lines of 256, 512 and 1024 points run
@@ -201,8 +205,12 @@ int pfgb_execute_many(pfgb_plan* plan, int direction, int normalise,
  * pfgb_backward, from src[i] to dst[i]) into one CUDA graph, replayed with a
  * single pfgb_batch_launch.  Covers the reference's collections of fields
  * (mul!/ldiv! over tuples and arrays, src/operations.jl:129-152) and any mix
- * of plans and sizes.  The buffers are fixed at creation; plans must outlive
- * the batch and must not run concurrently with it (they share scratch). */
+ * of plans and sizes.  The graph has one branch per plan, so transforms of
+ * different plans (independent fields) run concurrently; a transform waits
+ * for earlier ones of other plans whose buffers overlap its own (written
+ * then read, or read or written then written).  The buffers are fixed at
+ * creation; plans must outlive the batch and must not run concurrently with
+ * it (they share scratch). */
 typedef struct pfgb_batch pfgb_batch;
 int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* normalise,
                       void* const* dst, const void* const* src, int n, pfgb_batch** batch);
@@ -272,6 +280,20 @@ int pfgb_device_status(pfgb_plan* plan, void* stream, int32_t* flags);
  * eligible c2r passes in the TMA-fed form.  polls = 0, tma = 0 restore
  * normal execution. */
 int pfgb_plan_set_wait_test(pfgb_plan* plan, int polls, int tma);
+
+/* Planner wisdom (the counterpart of FFTW's wisdom, which the reference's
+ * FFTW planner accumulates and FFTW.jl exports and imports): plans created
+ * with autotune != 0 first look up the kernel choice of each measured pass
+ * (keyed by device, arithmetic and pass geometry) and measure only passes
+ * without an entry; every measurement is added.  pfgb_wisdom_export writes
+ * the entries to a text file, pfgb_wisdom_import merges a file written by
+ * it (PFGB_ERR_ARGUMENT for another format), pfgb_wisdom_forget clears them,
+ * pfgb_wisdom_stats reports the number of entries and of lookups answered
+ * since the last forget.  None of them needs a GPU. */
+int pfgb_wisdom_export(const char* path);
+int pfgb_wisdom_import(const char* path);
+int pfgb_wisdom_forget(void);
+int pfgb_wisdom_stats(int32_t* entries, int32_t* hits);
 
 /* Copies the message of the last failure on this thread into buf. Returns the
  * message length. */

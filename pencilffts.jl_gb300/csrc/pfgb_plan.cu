@@ -16,7 +16,10 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
+#include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -1456,6 +1459,59 @@ int pfgb_last_error(char* buf, size_t n) {
 
 static int autotune_passes(pfgb_plan* P);
 
+// ---------------------------------------------------------------------------
+// Planner wisdom: the kernel choices of the planner measurement, kept for
+// later plans of the same pass geometry on the same kind of device and
+// exported / imported as a text file (the image of FFTW's wisdom, which the
+// reference's FFTW planner accumulates under fftw_flags = FFTW.MEASURE).
+// ---------------------------------------------------------------------------
+static std::mutex g_wisdom_mutex;
+static std::map<std::string, int> g_wisdom;
+static int g_wisdom_hits = 0;
+static const char* kWisdomHeader = "pencilfft_gb300 wisdom 1";
+
+static std::string device_tag(int dev) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "unknown";
+  std::string n = prop.name;
+  for (auto& c : n)
+    if (c == ' ' || c == '|' || c == '\t') c = '_';
+  return n + "_sm" + std::to_string(prop.major) + std::to_string(prop.minor) + "x" +
+         std::to_string(prop.multiProcessorCount);
+}
+
+static std::string layout_tag(const Layout& L) {
+  std::ostringstream o;
+  for (int q = 0; q < L.D; ++q) o << L.size[L.perm[q]] << (q + 1 < L.D ? "," : "");
+  o << "p" << L.pitch0 << "e" << L.elt;
+  for (int q = 0; q < L.D; ++q) o << "/" << L.perm[q];
+  return o.str();
+}
+
+// Key of one measured choice: what was measured, device, arithmetic and the
+// pass geometry (operation, sign, length, both layouts, double-float form)
+static std::string wisdom_key(const pfgb_plan* P, const Pass& ps, const char* what) {
+  std::ostringstream o;
+  o << what << "|" << device_tag(P->device) << "|rb" << P->rb << "|pr" << P->precision << "|op" << ps.op
+    << "|s" << ps.sign << "|M" << ps.M << "|" << layout_tag(ps.lin) << "|" << layout_tag(ps.lout) << "|dd"
+    << ps.in_dd << ps.out_dd;
+  return o.str();
+}
+
+static bool wisdom_lookup(const std::string& key, int* variant) {
+  std::lock_guard<std::mutex> lock(g_wisdom_mutex);
+  auto it = g_wisdom.find(key);
+  if (it == g_wisdom.end()) return false;
+  *variant = it->second;
+  ++g_wisdom_hits;
+  return true;
+}
+
+static void wisdom_store(const std::string& key, int variant) {
+  std::lock_guard<std::mutex> lock(g_wisdom_mutex);
+  g_wisdom[key] = variant;
+}
+
 static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_only) {
   g_last_error.clear();
   if (!desc || !out) return fail(PFGB_ERR_ARGUMENT, "null argument");
@@ -1729,6 +1785,12 @@ static int autotune_passes(pfgb_plan* P) {
   for (auto* dir : {&P->fwd, &P->bwd}) {
     for (auto& ps : dir->passes) {
       if (!ps.fast || ps.op != OP_C2R || ps.tc || P->fx) continue;  // fx passes have one kernel
+      const std::string wkey = wisdom_key(P, ps, "c2r-tma");
+      int wv = 0;
+      if (wisdom_lookup(wkey, &wv)) {
+        ps.variant = wv;
+        continue;
+      }
       void* bin = nullptr;
       void* bout = nullptr;
       const size_t nin = (size_t)ps.lin.bytes(), nout = (size_t)ps.lout.bytes();
@@ -1768,6 +1830,7 @@ static int autotune_passes(pfgb_plan* P) {
         }
       }
       ps.variant = best[1] < best[0] ? 1 : 0;
+      if (!rc) wisdom_store(wkey, ps.variant);
       if (ea) cudaEventDestroy(ea);
       if (eb) cudaEventDestroy(eb);
       cudaFree(bin);
@@ -1780,6 +1843,12 @@ static int autotune_passes(pfgb_plan* P) {
   for (auto* dir : {&P->fwd, &P->bwd}) {
     for (auto& ps : dir->passes) {
       if (!ps.bs) continue;
+      const std::string wkey = wisdom_key(P, ps, "bluestein-generic");
+      int wv = 0;
+      if (wisdom_lookup(wkey, &wv)) {
+        ps.variant = wv;
+        continue;
+      }
       void* bin = nullptr;
       void* bout = nullptr;
       const size_t nin = (size_t)ps.lin.bytes(), nout = (size_t)ps.lout.bytes();
@@ -1821,6 +1890,7 @@ static int autotune_passes(pfgb_plan* P) {
         }
       }
       ps.variant = best[1] < best[0] ? 2 : -1;
+      if (!rc) wisdom_store(wkey, ps.variant);
       if (ea) cudaEventDestroy(ea);
       if (eb) cudaEventDestroy(eb);
       cudaFree(bin);
@@ -1829,6 +1899,55 @@ static int autotune_passes(pfgb_plan* P) {
     }
   }
   PFGB_CUDA(cudaMemset(P->emax_dev, 0, 16));  // exponent and error words
+  return PFGB_OK;
+}
+
+int pfgb_wisdom_export(const char* path) {
+  if (!path) return fail(PFGB_ERR_ARGUMENT, "null path");
+  std::lock_guard<std::mutex> lock(g_wisdom_mutex);
+  std::ofstream f(path);
+  if (!f) return fail(PFGB_ERR_ARGUMENT, std::string("cannot write wisdom file ") + path);
+  f << kWisdomHeader << "\n";
+  for (const auto& kv : g_wisdom) f << kv.second << "\t" << kv.first << "\n";
+  return f.good() ? PFGB_OK : fail(PFGB_ERR_ARGUMENT, std::string("error writing wisdom file ") + path);
+}
+
+int pfgb_wisdom_import(const char* path) {
+  if (!path) return fail(PFGB_ERR_ARGUMENT, "null path");
+  std::ifstream f(path);
+  if (!f) return fail(PFGB_ERR_ARGUMENT, std::string("cannot read wisdom file ") + path);
+  std::string line;
+  if (!std::getline(f, line) || line != kWisdomHeader)
+    return fail(PFGB_ERR_ARGUMENT, std::string("not a pencilfft_gb300 wisdom file: ") + path);
+  std::map<std::string, int> got;
+  int lineno = 1;
+  while (std::getline(f, line)) {
+    ++lineno;
+    if (line.empty()) continue;
+    const size_t tab = line.find('\t');
+    char* end = nullptr;
+    const long v = tab == std::string::npos ? 0 : std::strtol(line.c_str(), &end, 10);
+    if (tab == std::string::npos || tab == 0 || end != line.c_str() + tab || v < -1 || v > 2 || tab + 1 >= line.size())
+      return fail(PFGB_ERR_ARGUMENT, "malformed wisdom line " + std::to_string(lineno) + " in " + path);
+    got[line.substr(tab + 1)] = (int)v;
+  }
+  std::lock_guard<std::mutex> lock(g_wisdom_mutex);
+  for (const auto& kv : got) g_wisdom[kv.first] = kv.second;
+  return PFGB_OK;
+}
+
+int pfgb_wisdom_forget(void) {
+  std::lock_guard<std::mutex> lock(g_wisdom_mutex);
+  g_wisdom.clear();
+  g_wisdom_hits = 0;
+  return PFGB_OK;
+}
+
+int pfgb_wisdom_stats(int32_t* entries, int32_t* hits) {
+  if (!entries || !hits) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lock(g_wisdom_mutex);
+  *entries = (int32_t)g_wisdom.size();
+  *hits = (int32_t)g_wisdom_hits;
   return PFGB_OK;
 }
 
@@ -1961,11 +2080,16 @@ int pfgb_backward(pfgb_plan* P, void* dst, const void* src, void* stream, int no
 
 struct pfgb_batch {
   cudaStream_t cap = nullptr;
+  std::vector<cudaStream_t> side;  // branches of the recorded graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int n = 0;
 };
 
+// Records the batch as a graph with one branch per plan (the transforms of a
+// plan share its scratch and stay in order on their branch); an operation
+// also waits for every earlier operation of another branch whose buffers it
+// reads or writes where that one wrote, or writes where that one read.
 int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* normalise,
                       void* const* dst, const void* const* src, int n, pfgb_batch** out) {
   g_last_error.clear();
@@ -1978,24 +2102,88 @@ int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* 
     int rc = check_buffers(plans[i], dst[i], src[i], direction[i] >= 0);
     if (rc) return rc;
   }
+  // byte ranges read and written by each operation
+  struct Range {
+    const char* a;
+    int64_t n;
+  };
+  std::vector<Range> rd(n), wr(n);
+  for (int i = 0; i < n; ++i) {
+    const pfgb_plan* P = plans[i];
+    const bool f = direction[i] >= 0;
+    const int64_t bi = P->inplace ? P->inplace_bytes : (f ? P->in_layout.bytes() : P->out_layout.bytes());
+    const int64_t bo = P->inplace ? P->inplace_bytes : (f ? P->out_layout.bytes() : P->in_layout.bytes());
+    rd[i] = {static_cast<const char*>(src[i]), bi};
+    wr[i] = {static_cast<const char*>(dst[i]), bo};
+  }
+  auto overlap = [](const Range& x, const Range& y) { return x.a < y.a + y.n && y.a < x.a + x.n; };
   pfgb_batch* B = new pfgb_batch();
   B->n = n;
+  std::vector<cudaEvent_t> events;
   auto cleanup = [&](int rc) {
-    if (B->exec) cudaGraphExecDestroy(B->exec);
-    if (B->graph) cudaGraphDestroy(B->graph);
-    if (B->cap) cudaStreamDestroy(B->cap);
-    delete B;
+    for (auto ev : events) cudaEventDestroy(ev);
+    if (rc) {
+      if (B->exec) cudaGraphExecDestroy(B->exec);
+      if (B->graph) cudaGraphDestroy(B->graph);
+      for (auto st : B->side) cudaStreamDestroy(st);
+      if (B->cap) cudaStreamDestroy(B->cap);
+      delete B;
+    }
     return rc;
+  };
+  auto new_event = [&](cudaEvent_t* ev) {
+    cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) events.push_back(*ev);
+    return e;
   };
   cudaError_t e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+  // one branch per distinct plan
+  std::vector<int> branch(n);
+  std::map<const pfgb_plan*, int> plan_branch;
+  for (int i = 0; i < n; ++i) {
+    auto it = plan_branch.find(plans[i]);
+    if (it == plan_branch.end()) {
+      cudaStream_t st = nullptr;
+      e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+      B->side.push_back(st);
+      it = plan_branch.emplace(plans[i], (int)B->side.size() - 1).first;
+    }
+    branch[i] = it->second;
+  }
   e = cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e)));
   int rc = PFGB_OK;
+  cudaEvent_t fork = nullptr;
+  if ((e = new_event(&fork)) != cudaSuccess || (e = cudaEventRecord(fork, B->cap)) != cudaSuccess)
+    rc = fail(PFGB_ERR_CUDA, std::string("batch fork event: ") + cudaGetErrorString(e));
+  for (auto st : B->side)
+    if (!rc && (e = cudaStreamWaitEvent(st, fork, 0)) != cudaSuccess)
+      rc = fail(PFGB_ERR_CUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
+  std::vector<cudaEvent_t> done(n, nullptr);
   for (int i = 0; i < n && !rc; ++i) {
     pfgb_plan* P = plans[i];
-    rc = direction[i] >= 0 ? execute(P, P->fwd, dst[i], src[i], B->cap, false, 1)
-                           : execute(P, P->bwd, dst[i], src[i], B->cap, normalise && normalise[i], -1);
+    cudaStream_t st = B->side[branch[i]];
+    for (int j = 0; j < i && !rc; ++j) {
+      if (branch[j] == branch[i]) continue;
+      if (overlap(wr[j], rd[i]) || overlap(wr[j], wr[i]) || overlap(rd[j], wr[i]))
+        if ((e = cudaStreamWaitEvent(st, done[j], 0)) != cudaSuccess)
+          rc = fail(PFGB_ERR_CUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
+    }
+    if (rc) break;
+    rc = direction[i] >= 0 ? execute(P, P->fwd, dst[i], src[i], st, false, 1)
+                           : execute(P, P->bwd, dst[i], src[i], st, normalise && normalise[i], -1);
+    if (!rc && ((e = new_event(&done[i])) != cudaSuccess || (e = cudaEventRecord(done[i], st)) != cudaSuccess))
+      rc = fail(PFGB_ERR_CUDA, std::string("batch event: ") + cudaGetErrorString(e));
+  }
+  // join every branch into the capturing stream
+  for (auto st : B->side) {
+    cudaEvent_t j = nullptr;
+    if ((e = new_event(&j)) != cudaSuccess || (e = cudaEventRecord(j, st)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(B->cap, j, 0)) != cudaSuccess) {
+      if (!rc) rc = fail(PFGB_ERR_CUDA, std::string("batch join: ") + cudaGetErrorString(e));
+    }
   }
   cudaGraph_t g = nullptr;
   e = cudaStreamEndCapture(B->cap, &g);
@@ -2004,6 +2192,7 @@ int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* 
   if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e)));
   e = cudaGraphInstantiate(&B->exec, B->graph, 0);
   if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)));
+  cleanup(PFGB_OK);
   *out = B;
   return PFGB_OK;
 }
@@ -2019,6 +2208,7 @@ int pfgb_batch_destroy(pfgb_batch* B) {
   if (!B) return PFGB_OK;
   if (B->exec) cudaGraphExecDestroy(B->exec);
   if (B->graph) cudaGraphDestroy(B->graph);
+  for (auto st : B->side) cudaStreamDestroy(st);
   if (B->cap) cudaStreamDestroy(B->cap);
   delete B;
   return PFGB_OK;

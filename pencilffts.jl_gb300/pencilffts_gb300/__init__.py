@@ -8,7 +8,8 @@ from . import transforms as Transforms
 from ._lib import ArgumentError, LibraryError, load as load_library
 from .plans import (FFTW_ESTIMATE, FFTW_EXHAUSTIVE, FFTW_MEASURE, FFTW_PATIENT, Batch,
                     ManyPencilArray, Pencil, PencilArray, PencilFFTPlan, Val,
-                    allocate_input, allocate_output, bmul_, gather, is_inplace,
+                    allocate_input, allocate_output, bmul_, export_wisdom, forget_wisdom,
+                    gather, import_wisdom, is_inplace, wisdom_stats,
                     ldiv, ldiv_, ldiv_curl_, ldiv_deriv_sum_, ldiv_divergence_, mul_,
                     plan_query, scale_factor)
 
@@ -16,6 +17,7 @@ __all__ = [
     "Transforms", "Batch", "ArgumentError", "LibraryError", "load_library", "ManyPencilArray",
     "Pencil", "PencilArray", "PencilFFTPlan", "Val", "allocate_input", "allocate_output",
     "bmul_", "gather", "is_inplace", "ldiv", "ldiv_", "ldiv_curl_", "ldiv_deriv_sum_",
-    "ldiv_divergence_", "mul_", "plan_query", "scale_factor",
+    "ldiv_divergence_", "mul_", "plan_query", "scale_factor", "export_wisdom", "import_wisdom",
+    "forget_wisdom", "wisdom_stats",
     "FFTW_ESTIMATE", "FFTW_MEASURE", "FFTW_PATIENT", "FFTW_EXHAUSTIVE",
 ]

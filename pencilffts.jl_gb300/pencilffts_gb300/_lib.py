@@ -99,6 +99,10 @@ SIGNATURES = {
     "pfgb_fft1d_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _vp, _vp, _vp]),
     "pfgb_device_status": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(ctypes.c_int32)]),
     "pfgb_plan_set_wait_test": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "pfgb_wisdom_export": (ctypes.c_int, [ctypes.c_char_p]),
+    "pfgb_wisdom_import": (ctypes.c_int, [ctypes.c_char_p]),
+    "pfgb_wisdom_forget": (ctypes.c_int, []),
+    "pfgb_wisdom_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "pfgb_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "pfgb_version": (ctypes.c_char_p, []),
 }

@@ -12,6 +12,7 @@ Julia and ``ldiv(plan, uF)`` (or ``plan.ldiv(uF)``) is ``plan \\ uF``.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 from typing import Sequence
 
@@ -610,6 +611,34 @@ class Batch:
             except Exception:
                 pass
             self._h = None
+
+
+def export_wisdom(path) -> None:
+    """Writes the planner's measured kernel choices to ``path`` (FFTW.jl's
+    ``export_wisdom``)."""
+    L = _lib.load()
+    _lib.check(L.pfgb_wisdom_export(os.fsencode(path)), "pfgb_wisdom_export")
+
+
+def import_wisdom(path) -> None:
+    """Merges kernel choices from a file written by ``export_wisdom``
+    (FFTW.jl's ``import_wisdom``); later plans with ``fftw_flags`` other than
+    ``FFTW_ESTIMATE`` use them instead of measuring."""
+    L = _lib.load()
+    _lib.check(L.pfgb_wisdom_import(os.fsencode(path)), "pfgb_wisdom_import")
+
+
+def forget_wisdom() -> None:
+    """Clears the planner's kernel choices (FFTW.jl's ``forget_wisdom``)."""
+    _lib.load().pfgb_wisdom_forget()
+
+
+def wisdom_stats():
+    """(entries, lookups answered since the last forget)."""
+    L = _lib.load()
+    e, h = ctypes.c_int32(0), ctypes.c_int32(0)
+    _lib.check(L.pfgb_wisdom_stats(ctypes.byref(e), ctypes.byref(h)), "pfgb_wisdom_stats")
+    return e.value, h.value
 
 
 def mul_(dst, plan: PencilFFTPlan, src, *, deriv=None):

@@ -157,3 +157,37 @@ def test_autotune_measure(cuda, real):
     w, wref = plan.ldiv(v), ref.ldiv(vref)
     assert np.array_equal(w.to_logical(), wref.to_logical())
     assert plan.device_status() == 0
+
+
+def test_batch_branches_respect_buffer_order(cuda):
+    """A batch records one graph branch per plan; operations of different
+    plans that share buffers are ordered: B = F(A) then C = F(B) (read after
+    write) and A overwritten by F(D) only after F(A) read it (write after
+    read)."""
+    dims = (32, 24, 20)
+    p1 = P.PencilFFTPlan(dims, T.FFT(), np.float64)
+    p2 = P.PencilFFTPlan(dims, T.FFT(), np.float64)
+    p3 = P.PencilFFTPlan(dims, T.FFT(), np.float64)
+    rng = np.random.default_rng(17)
+    xa = rng.standard_normal(dims) + 1j * rng.standard_normal(dims)
+    xd = rng.standard_normal(dims) + 1j * rng.standard_normal(dims)
+    A, D = input_array(p1, xa), input_array(p1, xd)
+    B, C = p1.allocate_output(), p1.allocate_output()
+    # C = F(B) needs B in the input layout of p2: the output of p1 is the
+    # reversed layout, so p2 reads it as a plan on the reversed dimensions
+    p2 = P.PencilFFTPlan(tuple(reversed(dims)), T.FFT(), np.float64, permute_dims=False)
+    Bv = P.PencilArray(p2.pencil_input(), B.data, B.dtype)
+    Cv = P.PencilArray(p2.pencil_output(), C.data, C.dtype)
+    # F(D) written over A's buffer, in p3's output layout
+    Av = P.PencilArray(p3.pencil_output(), A.data.view(p3.pencil_output().memory_shape()), A.dtype)
+    batch = P.Batch([(P.mul_, B, p1, A), (P.mul_, Cv, p2, Bv), (P.mul_, Av, p3, D)])
+    batch.launch()
+    import torch
+    torch.cuda.synchronize()
+    o1 = oracle_plan(p1)
+    fa = o1.forward(xa)
+    assert rel(B.to_logical(), fa) <= 1e-13
+    # C holds the 3D FFT of F(A) taken in memory order (reversed dimensions)
+    fb_mem = np.fft.fftn(fa.transpose(2, 1, 0))
+    assert rel(Cv.to_logical(), fb_mem) <= 1e-13
+    assert rel(Av.to_logical(), o1.forward(xd)) <= 1e-13
