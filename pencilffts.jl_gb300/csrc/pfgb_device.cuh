@@ -39,6 +39,10 @@ enum PassOp : int {
   // register Stockham pass only: a c2c pass whose input is the sum over up
   // to kMaxTerms sources of c_t i k_t src_t (fused divergence / curl)
   OP_CSUM = 7,
+  // register Stockham pass only: the first pass of a line split in two
+  // (lines longer than one pass takes): c2c along n2 whose outputs are
+  // multiplied by W_M^(n1 k2), n1 the index along the line's other part
+  OP_C2CT = 8,
 };
 
 // FFTW r2r kind codes.

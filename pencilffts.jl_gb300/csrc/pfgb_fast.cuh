@@ -38,6 +38,11 @@ struct FastArgs {
   const void* bs_chirp;
   const void* bs_filt;
   Div31 div_m;
+  // OP_C2CT (first pass of a split line of M = M1 * M2 points): outputs times
+  // exp(sign 2 pi i n1 k2 / M) from t4_tab (M entries), n1 the index along
+  // the dimension of role t4_role (1 tile, 2 + o outer)
+  const void* t4_tab;
+  int t4_role;
   int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R
   int r2r_odd;     // OP_X00C / OP_X00R: 0 REDFT00 (even extension), 1 RODFT00 (odd)
   int n_in, n_out;
@@ -564,7 +569,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       emax_out = emax + a.emax_shift;
     }
   }
-  if constexpr (OP == OP_C2C) {
+  if constexpr (OP == OP_C2C || OP == OP_C2CT) {
     if (IO::kDD && IN_DD) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
       // exponents of the elements' first-pass lines, loaded ahead of the data
@@ -802,8 +807,14 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
     }
   }
+  if constexpr (OP == OP_C2CT) {
+    // the split line's twiddles W_M^(n1 k2), k2 = b + r T, before any store
+    const int64_t n1 = a.t4_role == 1 ? t0 + p : outer_index(a, (unsigned)bid, a.t4_role - 2);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = tw_mul<R, SIGN>(v[r], a.t4_tab, (int)(n1 * (int64_t)(b + r * T)));
+  }
   if (a.store_direct && OP != OP_R2C) {
-    if constexpr (OP == OP_C2C || OP == OP_CSUM) {
+    if constexpr (OP == OP_C2C || OP == OP_CSUM || OP == OP_C2CT) {
       if (p < nvalid) {
         if (IO::kDD && OUT_DD) {
           float4* out = reinterpret_cast<float4*>(a.out) + ooff + (int64_t)p * a.out_st;
@@ -884,7 +895,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   // output exponent of complex line i (the first pass of a run scales lines
   // separately; the loops below write other threads' lines)
   auto line_emax_out = [&](int i) { return IO::kDD && a.self_scale ? lexp[i] + a.emax_shift : emax_out; };
-  if constexpr (OP == OP_C2C || OP == OP_CSUM) {
+  if constexpr (OP == OP_C2C || OP == OP_CSUM || OP == OP_C2CT) {
     MC* out = reinterpret_cast<MC*>(a.out) + ooff;
     const int tot = TW * M;
     for (int e = tid; e < tot; e += nth) {

@@ -8,6 +8,7 @@ int launch_fast_f32_c2r_0(int logm, int sign, const FastArgs& A, int64_t grid, c
 int launch_fast_f32_x00c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_f32_x00r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_f32_csum_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_f32_c2ct_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
 int launch_fast_f32_c2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   return launch_fast_op<float, OP_C2C, 0>(logm, sign, A, grid, s);
@@ -24,6 +25,7 @@ int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStr
     case OP_X00C * 4 + 0: return launch_fast_f32_x00c_0(logm, sign, A, grid, s);
     case OP_X00R * 4 + 0: return launch_fast_f32_x00r_0(logm, sign, A, grid, s);
     case OP_CSUM * 4 + 0: return launch_fast_f32_csum_0(logm, sign, A, grid, s);
+    case OP_C2CT * 4 + 0: return launch_fast_f32_c2ct_0(logm, sign, A, grid, s);
     default: return PFGB_ERR_UNSUPPORTED;
   }
 }

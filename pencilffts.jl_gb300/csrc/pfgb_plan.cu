@@ -55,7 +55,9 @@ int fail_cuda(cudaError_t e, const char* what) {
       return fail(PFGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-constexpr int kMaxD = PFGB_MAX_DIMS + PFGB_MAX_EXTRA;
+// logical dimensions of a layout: transformed + extra, plus one for the
+// second part of a line split in two (the two passes of a long line)
+constexpr int kMaxD = PFGB_MAX_DIMS + PFGB_MAX_EXTRA + 1;
 constexpr int kMaxLc = 8192;  // longest line held in shared memory
 
 // ---------------------------------------------------------------------------
@@ -122,6 +124,13 @@ struct Pass {
   // convolution length 2^logl (ftw holds its twiddles), chirp and filter
   // tables; the generic kernel's geometry is kept (g_*) for executions it
   // must take (a fused derivative on this pass)
+  // line split in two (lines longer than one register pass takes): both
+  // passes carry `four`; the first (t4_dim >= 0) multiplies its outputs by
+  // W_M^(n1 k2), n1 the index along dimension t4_dim, M = t4_M
+  bool four = false;
+  int t4_dim = -1;
+  int64_t t4_M = 0;
+  const void* t4_tab = nullptr;
   bool bs = false;
   int logl = 0;
   const void* bs_chirp = nullptr;
@@ -631,7 +640,11 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
       M <= 4096 && (M & (M - 1)) == 0 &&
       !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
     ps.fast = true;
-    ps.fop = x00 ? (ps.op == OP_R2R_C ? OP_X00C : OP_X00R) : ps.op;
+    ps.fop = x00 ? (ps.op == OP_R2R_C ? OP_X00C : OP_X00R) : ps.t4_dim >= 0 ? OP_C2CT : ps.op;
+    if (ps.t4_dim >= 0) {
+      rc = upload_fast_table(P, (int)ps.t4_M, &ps.t4_tab);
+      if (rc) return rc;
+    }
     ps.logm = 0;
     while ((1 << ps.logm) < M) ++ps.logm;
     rc = upload_fast_table(P, M, &ps.ftw);
@@ -642,7 +655,7 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
     ps.lines = packed ? 2 * ps.clines : ps.clines;
     ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm, ps.fop) : fast_threads<float>(ps.logm, ps.fop);
     ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm, ps.fop) : fast_smem<float>(ps.logm, ps.fop);
-    if (P->precision == PFGB_PRECISION_TC_SPLIT && ps.op == OP_C2C && tc_lines(ps.logm) > 0) {
+    if (P->precision == PFGB_PRECISION_TC_SPLIT && ps.fop == OP_C2C && tc_lines(ps.logm) > 0) {
       ps.tc = true;
       ps.clines = ps.lines = tc_lines(ps.logm);
       rc = upload_tc_table(P, ps.logm, ps.sign, &ps.tcb);
@@ -740,6 +753,22 @@ static int tile_dim(const Pass& ps) {
   if (!a_fast_in) return ps.lin.perm[0];
   if (!a_fast_out) return ps.lout.perm[0];
   return ps.lin.D > 1 ? ps.lin.perm[1] : -1;
+}
+
+// Role of logical dimension dim in a pass: 0 the axis, 1 the tile dimension,
+// 2 + o the o-th outer dimension (input memory order), -1 absent.
+static int pass_role(const Pass& ps, int dim) {
+  if (dim == ps.axis) return 0;
+  const int t = tile_dim(ps);
+  if (dim == t) return 1;
+  int o = 0;
+  for (int q = 0; q < ps.lin.D; ++q) {
+    const int d = ps.lin.perm[q];
+    if (d == ps.axis || d == t) continue;
+    if (d == dim) return 2 + o;
+    ++o;
+  }
+  return -1;
 }
 
 // Complex lines of a fast pass along its tile dimension (two real lines per
@@ -909,6 +938,8 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.out = out;
   F.tw = ps.ftw;
   F.tw2 = ps.ftw2;
+  F.t4_tab = ps.t4_tab;
+  F.t4_role = ps.t4_dim >= 0 ? pass_role(ps, ps.t4_dim) : 0;
   F.op = ps.fop;
   F.r2r_odd = ps.r2r_kind == K_RODFT00 ? 1 : 0;
   F.n_in = A.n_in;
@@ -1143,6 +1174,82 @@ static bool inplace_ok(const Pass& ps) {
   return ps.lin.elt == ps.lout.elt && ps.lin.size[a] == ps.lout.size[a];
 }
 
+// A line length one register pass takes: a power of two up to 4096 (fast
+// pass; lengths below 8 through Bluestein), 3 * 2^k or 5 * 2^k with
+// 8 <= 2^k <= 512 (mixed-radix pass), or any length up to 2048 (Bluestein).
+static bool one_pass_length(int64_t n) {
+  if (n < 2 || n > 4096) return false;
+  if ((n & (n - 1)) == 0) return true;
+  for (int r0 : {3, 5}) {
+    const int64_t m = n / r0;
+    if (n % r0 == 0 && m >= 8 && m <= 512 && (m & (m - 1)) == 0) return true;
+  }
+  return n <= 2048;
+}
+
+// Inserts dimension v right after (after = true) or before dimension a in a
+// layout's memory order, a keeping m1 points and v taking m2 (a line of
+// m1 * m2 points seen as two dimensions).  false if a is the fastest
+// dimension and padded.
+static bool split_layout(const Layout& L, int a, int v, int64_t m1, int64_t m2, bool after, Layout& out) {
+  if (L.perm[0] == a && L.pitch0 != L.size[a]) return false;
+  out = L;
+  out.D = L.D + 1;
+  out.size[a] = m1;
+  out.size[v] = m2;
+  int q = 0;
+  for (int i = 0; i < L.D; ++i) {
+    if (L.perm[i] == a) {
+      if (after) { out.perm[q++] = a; out.perm[q++] = v; }
+      else { out.perm[q++] = v; out.perm[q++] = a; }
+    } else {
+      out.perm[q++] = L.perm[i];
+    }
+  }
+  out.pitch0 = out.size[out.perm[0]];
+  if (L.perm[0] != a) out.pitch0 = L.pitch0;
+  return true;
+}
+
+// Long c2c lines (M > 4096): M = M1 * M2 with M2 = 2^k (8 <= 2^k <= 4096)
+// and M1 a one-pass length, two passes: with n = n1 + M1 n2 and
+// k = k2 + M2 k1, pass A transforms n2 (the layout's dimension a split as
+// (n1 faster, n2)) and multiplies by W_M^(n1 k2); pass B transforms n1 and
+// writes X[k2 + M2 k1] through the output layout split as (k2 faster, k1).
+// Chooses the split with the most balanced M1, M2; false if none.
+static bool split_long_pass(const Pass& ps, Pass& A, Pass& B) {
+  if (ps.pk != PK_TRANSFORM || ps.op != OP_C2C) return false;
+  const int a = ps.axis;
+  const int64_t M = ps.lin.size[a];
+  if (M <= 4096 || M > (int64_t{1} << 24)) return false;
+  int64_t best_m2 = 0;
+  double best = 1e9;
+  for (int64_t m2 = 8; m2 <= 4096 && m2 < M; m2 *= 2) {
+    if (M % m2 || !one_pass_length(M / m2)) continue;
+    const double d = std::fabs(std::log2((double)(M / m2)) - std::log2((double)m2));
+    if (d < best) { best = d; best_m2 = m2; }
+  }
+  if (!best_m2) return false;
+  const int64_t m2 = best_m2, m1 = M / m2;
+  const int v = ps.lin.D;  // the split's second dimension
+  Layout lin_s, lout_s;
+  if (!split_layout(ps.lin, a, v, m1, m2, true, lin_s)) return false;
+  if (!split_layout(ps.lout, a, v, m1, m2, false, lout_s)) return false;
+  A = ps;
+  A.four = true;
+  A.axis = v;
+  A.lin = lin_s;
+  A.lout = lin_s;  // the intermediate keeps the input's order (in place possible)
+  A.t4_dim = a;
+  A.t4_M = M;
+  B = ps;
+  B.four = true;
+  B.axis = a;
+  B.lin = lin_s;
+  B.lout = lout_s;
+  return true;
+}
+
 struct Step {  // one transform of the reference's per-dimension loop
   int axis, op, r2r, sign;
 };
@@ -1251,6 +1358,20 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
     for (int q = 0; q < N; ++q) sizes[q] = nsz[q];
     cplx = ncx;
   }
+  // lines longer than one register pass: two passes each
+  if (!(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+    std::vector<Pass> split;
+    for (const Pass& ps : passes) {
+      Pass A, B;
+      if (split_long_pass(ps, A, B)) {
+        split.push_back(A);
+        split.push_back(B);
+      } else {
+        split.push_back(ps);
+      }
+    }
+    passes.swap(split);
+  }
   if (passes.empty()) {
     if (!P->inplace) {
       Pass c;
@@ -1345,6 +1466,8 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
     if (dpass < 0 || dir.passes[dpass].op != OP_C2C)
       return fail(PFGB_ERR_UNSUPPORTED, "the fused derivative needs a complex-to-complex pass at that end "
                                         "of the plan");
+    if (dir.passes[dpass].four)
+      return fail(PFGB_ERR_UNSUPPORTED, "the fused derivative is not available on a line split in two passes");
   }
   for (int i = 0; i < m; ++i) {
     const Pass& ps = dir.passes[i];
@@ -1376,10 +1499,11 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
     } else if (ps.fast) {
       FastArgs F;
       int64_t grid = 0;
+      const bool fxp = fxrun && !ps.four;  // split lines run in double-float
       int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr,
-                              fxrun ? i : -1);
+                              fxp ? i : -1);
       if (rc) return rc;
-      if (fxrun) {
+      if (fxp) {
         rc = launch_fast_fx(ps.logm, ps.sign, F, grid, s);
       } else if (ps.tc) {
         F.total = grid;
@@ -1636,7 +1760,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
       auto& v = dir->passes;
       // passes that exchange dd-form data with their neighbours (packed real
       // R2R lines always read and write doubles)
-      auto chains = [](const Pass& q) { return q.fast && q.fop != OP_X00R; };
+      auto chains = [](const Pass& q) { return q.fast && q.fop != OP_X00R && !q.four; };
       for (size_t i = 0; i < v.size(); ++i) {
         if (!v[i].fast) continue;
         const bool prev = chains(v[i]) && i > 0 && chains(v[i - 1]);
@@ -1681,7 +1805,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
           F.out_dd = ps.out_dd ? 1 : 0;
           rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, 0, nullptr)
                           : launch_fast_f32(ps.logm, ps.sign, F, 0, nullptr);
-          if (!rc && P->fx) rc = launch_fast_fx(ps.logm, ps.sign, F, 0, nullptr);
+          if (!rc && P->fx && !ps.four) rc = launch_fast_fx(ps.logm, ps.sign, F, 0, nullptr);
           if (!rc && PFGB_FAST_TMA)
             rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, nullptr)
                             : launch_fast_tma_f32(ps.logm, ps.sign, F, nullptr);

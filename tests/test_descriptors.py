@@ -196,3 +196,14 @@ def test_fftw_flags_select_measurement():
     assert _autotune_from(P.FFTW_ESTIMATE, True) == 1
     assert _autotune_from(P.FFTW_MEASURE, False) == 0
     P.plan_query((64, 48, 32), T.RFFT())  # host-only analysis never measures
+
+
+def test_long_c2c_lines_take_two_passes():
+    """c2c lines above 4096 points are split in two register passes (host
+    plan query, no device); long r2c lines stay unsupported."""
+    info = P.plan_query((16384,), T.FFT(), np.float64)
+    assert info.n_passes_forward == 2 and info.n_passes_backward == 2
+    info = P.plan_query((8, 1 << 20), T.FFT(), np.float32)
+    assert info.n_passes_forward == 3
+    with pytest.raises(P.LibraryError):
+        P.plan_query((16384,), T.RFFT(), np.float64)
