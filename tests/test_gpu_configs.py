@@ -162,9 +162,10 @@ def test_c4_rfft_1024_f32_properties(cuda, precision):
 
 
 def test_c5_vector_gradient_384(cuda):
-    """3-component Float32 field 384^3: forward, multiply by i k (spectral
-    gradient of each component along x), backward; against the oracle."""
-    import torch
+    """3-component Float32 field 384^3 (384 = 3 * 128, the mixed-radix pass):
+    forward, then the derivative of component c along dimension c fused into
+    the first backward pass (ldiv_ with deriv), and the divergence of the
+    field as one fused backward transform; against the oracle."""
     n = 384
     dims = (n, n, n)
     plan = P.PencilFFTPlan(dims, T.RFFT(), np.float32)
@@ -174,23 +175,43 @@ def test_c5_vector_gradient_384(cuda):
     for c, x in zip(u, comps):
         c.copy_from_logical(x)
     uF = plan * u
-    kx = torch.arange(n // 2 + 1, device="cuda", dtype=torch.float32)
-    for c in uF:  # d/dx in spectral space: i kx (output memory order (x, y, z))
-        c.data.mul_((1j * kx).to(torch.complex64)[:, None, None])
-    du = plan.ldiv(uF)
+    L = 2 * np.pi
+    du = plan.allocate_input(P.Val(3))
+    for c in range(3):
+        P.ldiv_(du[c], plan, uF[c], deriv=(c + 1, L))
     orc = oracle_plan(plan)
-    kxl = np.arange(n // 2 + 1)[:, None, None]
-    for c, x in zip(du, comps):
-        ref = orc.ldiv(orc.forward(x) * (1j * kxl))
-        assert rel(c.to_logical(), ref) <= 2e-6
+    specs = [orc.forward(x) for x in comps]
+    for c in range(3):
+        ref = orc.ldiv(specs[c] * O.wavenumbers(orc, c, L))
+        assert rel(du[c].to_logical(), ref) <= 2e-6
+    div = plan.allocate_input()
+    P.ldiv_divergence_(div, plan, uF, (L, L, L))
+    ref = orc.ldiv(sum(specs[c] * O.wavenumbers(orc, c, L) for c in range(3)))
+    assert rel(div.to_logical(), ref) <= 2e-6
 
 
 def test_c5_batch_of_64_uneven(cuda):
+    """64 independent Float32 r2c + c2r round trips of sizes drawn from
+    48..192 per axis (mixed radices, primes through Bluestein), recorded into
+    one batch (one CUDA graph, one branch per field) and launched once;
+    every field against the oracle."""
+    import torch
     rng = np.random.default_rng(2024)
     sizes = [tuple(int(s) for s in rng.integers(48, 193, 3)) for _ in range(64)]
-    for i, dims in enumerate(sizes):
+    plans, arrays, xs = [], [], []
+    for dims in sizes:
         plan = P.PencilFFTPlan(dims, T.RFFT(), np.float32)
         x = rng.standard_normal(dims).astype(np.float32)
-        out, back = run_fwd_bwd(plan, x)
-        assert rel(out, oracle_plan(plan).forward(x)) <= 2e-6, dims
-        assert rel(back, x) <= 2e-6, dims
+        u, v, w = input_array(plan, x), plan.allocate_output(), plan.allocate_input()
+        plans.append(plan)
+        arrays.append((u, v, w))
+        xs.append(x)
+    ops = []
+    for plan, (u, v, w) in zip(plans, arrays):
+        ops += [(P.mul_, v, plan, u), (P.ldiv_, w, plan, v)]
+    batch = P.Batch(ops)
+    batch.launch()
+    torch.cuda.synchronize()
+    for plan, (u, v, w), x, dims in zip(plans, arrays, xs, sizes):
+        assert rel(v.to_logical(), oracle_plan(plan).forward(x)) <= 2e-6, dims
+        assert rel(w.to_logical(), x) <= 2e-6, dims

@@ -162,5 +162,5 @@ def test_1d_lengths(cuda, n, real):
     """Mixed radices, primes (Bluestein) and long lines along one axis, batched."""
     plan = P.PencilFFTPlan((n, 5), (T.FFT(), T.NoTransform()), real)
     check_plan(plan)
-    plan = P.PencilFFTPlan((3, n), (T.NoTransform(), T.RFFT()) if False else (T.FFT(), T.FFT()), real)
+    plan = P.PencilFFTPlan((3, n), (T.FFT(), T.FFT()), real)
     check_plan(plan)
