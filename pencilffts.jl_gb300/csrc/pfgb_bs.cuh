@@ -23,13 +23,15 @@ template <typename R>
 __host__ __device__ constexpr int bs_threads(int logl) {
   return fast_threads<R>(logl, OP_C2C);
 }
+// 8 points a thread (the register stages' default), whatever the power-of-two
+// pass uses for this length
 template <typename R>
 __host__ __device__ constexpr int bs_tw(int logl) {
-  return fast_tw<R>(logl, OP_C2C);
+  return (bs_threads<R>(logl) * 8) >> logl > 0 ? (bs_threads<R>(logl) * 8) >> logl : 1;
 }
 template <typename R>
 __host__ __device__ constexpr size_t bs_smem(int logl) {
-  return fast_smem<R>(logl, OP_C2C);
+  return (size_t)bs_tw<R>(logl) * fast_pitch<R>(logl, OP_C2C) * sizeof(Cx<R>);
 }
 
 // x * w for a table entry w (Cx<R>: float (re, im) or dd (re.h, re.l, im.h, im.l))

@@ -151,6 +151,24 @@ __device__ __forceinline__ Cx<R> mul_ik(Cx<R> y, int64_t idx, int half, int64_t 
 #ifndef PFGB_FAST_THREADS_F32_LONG
 #define PFGB_FAST_THREADS_F32_LONG 1024
 #endif
+// Points per thread: 8, or 16 for Float32 lines of 2^PFGB_FAST_P16_LOGM
+// points and more.  With 16, the stages are radix-16 (dft16) and a 1024-point
+// line takes two shared-memory exchanges instead of three: the Float32
+// 1024-point passes are bound by those exchanges (MIO throttle, short
+// scoreboard and barrier stalls, 34-43% of DRAM throughput with 8 points).
+// Double-float lines keep 8 (their registers are full).
+#ifndef PFGB_FAST_P16_LOGM
+#define PFGB_FAST_P16_LOGM 10
+#endif
+// CTA size of the 16-point Float32 passes (8 lines of 1024 points a tile)
+#ifndef PFGB_FAST_THREADS_F32_P16
+#define PFGB_FAST_THREADS_F32_P16 512
+#endif
+template <typename R>
+__host__ __device__ constexpr int fast_pts(int logm) {
+  return sizeof(R) == 4 && logm >= PFGB_FAST_P16_LOGM ? 16 : 8;
+}
+
 // Operations of the fast pass that pack two real lines in one complex line.
 __host__ __device__ constexpr bool fast_packed(int op) {
   return op == OP_R2C || op == OP_C2R || op == OP_X00R;
@@ -158,13 +176,19 @@ __host__ __device__ constexpr bool fast_packed(int op) {
 
 template <typename R>
 __host__ __device__ constexpr int fast_threads(int logm, int op = OP_C2C) {
-  return sizeof(R) == 4 ? (logm >= 10 && op != OP_C2R ? PFGB_FAST_THREADS_F32_LONG : PFGB_FAST_THREADS_F32)
-                        : ((1 << logm) / 8 > PFGB_FAST_THREADS_DD ? (1 << logm) / 8 : PFGB_FAST_THREADS_DD);
+  return sizeof(R) == 4
+             ? (fast_pts<R>(logm) == 16
+                    ? ((1 << logm) / 16 > PFGB_FAST_THREADS_F32_P16 ? (1 << logm) / 16 : PFGB_FAST_THREADS_F32_P16)
+                : logm >= 10 && op != OP_C2R ? PFGB_FAST_THREADS_F32_LONG
+                                             : PFGB_FAST_THREADS_F32)
+             : ((1 << logm) / 8 > PFGB_FAST_THREADS_DD ? (1 << logm) / 8 : PFGB_FAST_THREADS_DD);
 }
 // complex lines per CTA for a line of 2^logm points (one line at least)
 template <typename R>
 __host__ __device__ constexpr int fast_tw(int logm, int op = OP_C2C) {
-  return (fast_threads<R>(logm, op) * 8) >> logm > 0 ? ((fast_threads<R>(logm, op) * 8) >> logm) : 1;
+  return (fast_threads<R>(logm, op) * fast_pts<R>(logm)) >> logm > 0
+             ? ((fast_threads<R>(logm, op) * fast_pts<R>(logm)) >> logm)
+             : 1;
 }
 // Shared-memory padding of the exchange buffer: one pad slot every 2^shift
 // elements plus `extra` slots per line.  Chosen from a bank model of the stage
@@ -268,9 +292,9 @@ __device__ __forceinline__ int sidx(int p, int pos) {
 // barrier per line (ids 1..lines, T a multiple of 32) or a warp barrier when
 // a warp holds whole lines.  With lines across the thread index (strided
 // axis, lanes along the tile dimension) every warp holds every line.
-template <typename R, int LOGM, int OP>
+template <typename R, int LOGM, int OP, int P = 8>
 __device__ __forceinline__ void line_sync(bool lanes_across_lines, int p) {
-  constexpr int T = (1 << LOGM) / 8;
+  constexpr int T = (1 << LOGM) / P;
   if (lanes_across_lines || T == fast_threads<R>(LOGM, OP)) {
     __syncthreads();
   } else if constexpr (T <= 32) {
@@ -280,36 +304,42 @@ __device__ __forceinline__ void line_sync(bool lanes_across_lines, int p) {
   }
 }
 
-template <typename R, int LOGM, int SIGN, int OP>
-__device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int b, const void* tw,
+// The register stages of a line of M = 2^LOGM points, P points a thread
+// (positions b + r M/P): radix-P stages (dft8 or dft16), then one radix-2,
+// 4 or 8 stage when log2 M is not a multiple of log2 P; outputs left in
+// natural order at the same positions.
+template <typename R, int LOGM, int SIGN, int OP, int P = 8>
+__device__ __forceinline__ void fast_stages(Cx<R> (&v)[P], Cx<R>* z, int p, int b, const void* tw,
                                             bool lanes_across_lines) {
   constexpr int M = 1 << LOGM;
-  constexpr int T = M / 8;
-  constexpr int S8 = LOGM / 3;
-  constexpr int REM = LOGM % 3;
-  constexpr int NST = S8 + (REM ? 1 : 0);
+  constexpr int T = M / P;
+  constexpr int LP = P == 16 ? 4 : 3;
+  constexpr int SP = LOGM / LP;
+  constexpr int REM = LOGM % LP;
+  constexpr int NST = SP + (REM ? 1 : 0);
   int Ls = 1;
 #pragma unroll
   for (int s = 0; s < NST; ++s) {
     const bool last = (s == NST - 1);
-    if (s < S8) {
+    if (s < SP) {
       const int j = b & (Ls - 1);
       if (Ls > 1) {
-        const int step = j * (M / (8 * Ls));
+        const int step = j * (M / (P * Ls));
 #pragma unroll
-        for (int r = 1; r < 8; ++r) v[r] = tw_mul<R, SIGN>(v[r], tw, r * step);
+        for (int r = 1; r < P; ++r) v[r] = tw_mul<R, SIGN>(v[r], tw, r * step);
       }
-      dft8<SIGN>(v);
+      if constexpr (P == 16) dft16<SIGN>(v);
+      else dft8<SIGN>(v);
       if (!last) {
-        Cx<R>* zw = z + sidx<R, LOGM, OP>(p, (b - j) * 8 + j);
+        Cx<R>* zw = z + sidx<R, LOGM, OP>(p, (b - j) * P + j);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * Ls)] = v[r];
+        for (int r = 0; r < P; ++r) zw[padded<R, LOGM>(r * Ls)] = v[r];
       }
-      Ls *= 8;
+      Ls *= P;
     } else {
-      // final radix-2 or radix-4 stage, Ls = M / RS: butterfly beta = b + r1 T
+      // final radix-2, 4 or 8 stage, Ls = M / RS: butterfly beta = b + r1 T
       constexpr int RS = 1 << (REM ? REM : 1);
-      constexpr int G = 8 / RS;
+      constexpr int G = P / RS;
 #pragma unroll
       for (int r1 = 0; r1 < G; ++r1) {
         const int beta = b + r1 * T;
@@ -317,17 +347,24 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[8], Cx<R>* z, int p, int 
         for (int q = 1; q < RS; ++q) v[r1 + q * G] = tw_mul<R, SIGN>(v[r1 + q * G], tw, q * beta);
         if constexpr (RS == 2) {
           dft2<SIGN>(v[r1], v[r1 + G]);
-        } else {
+        } else if constexpr (RS == 4) {
           dft4<SIGN>(v[r1], v[r1 + G], v[r1 + 2 * G], v[r1 + 3 * G]);
+        } else {
+          Cx<R> t[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) t[q] = v[r1 + q * G];
+          dft8<SIGN>(t);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v[r1 + q * G] = t[q];
         }
       }
     }
     if (!last) {
-      line_sync<R, LOGM, OP>(lanes_across_lines, p);
+      line_sync<R, LOGM, OP, P>(lanes_across_lines, p);
       const Cx<R>* zr = z + sidx<R, LOGM, OP>(p, b);
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = zr[padded<R, LOGM>(r * T)];
-      line_sync<R, LOGM, OP>(lanes_across_lines, p);
+      for (int r = 0; r < P; ++r) v[r] = zr[padded<R, LOGM>(r * T)];
+      line_sync<R, LOGM, OP, P>(lanes_across_lines, p);
     }
   }
 }
@@ -390,7 +427,9 @@ __device__ __forceinline__ Cx<R> apply_scale(Cx<R> y, const FastArgs& a) {
 // kernel variant: operation OP and IOM = dd input (bit 0) | dd output (bit 1)
 template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
-  return sizeof(R) == 4
+  return sizeof(R) == 4 && fast_pts<R>(logm) == 16
+             ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)  // 16 points: 64 registers a thread
+         : sizeof(R) == 4
              ? (op == OP_C2R && fast_threads<R>(logm, op) >= 1024
                     ? 1  // c2r at 1024 threads spills heavily at 32 registers
                     : ((op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS) <
@@ -436,11 +475,11 @@ __device__ __forceinline__ TileOrigin tile_origin(const FastArgs& a, unsigned bi
 // (self_scale): the largest biased exponent over the line (over the tile when
 // lines lie across the thread index).  The lines' leaders record it for the
 // next pass and fold it into the run's exponent word.  Called by all threads.
-template <typename R, int LOGM, int OP>
+template <typename R, int LOGM, int OP, int P = 8>
 __device__ __forceinline__ int line_exponent(unsigned emx, const FastArgs& a, unsigned bid, int64_t t0,
                                              int p, int nvalid_cl, bool lanes_across_lines) {
-  constexpr int T = (1 << LOGM) / 8;
-  constexpr int TW = fast_tw<R>(LOGM, OP);
+  constexpr int T = (1 << LOGM) / P;
+  constexpr int TW = (fast_threads<R>(LOGM, OP) * P) >> LOGM > 0 ? (fast_threads<R>(LOGM, OP) * P) >> LOGM : 1;
   __shared__ unsigned wmax[32];
   unsigned e;
   bool leader;
@@ -544,7 +583,8 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   using MR = typename IO::MR;
   using MC = typename IO::MC;
   constexpr int M = 1 << LOGM;
-  constexpr int T = M / 8;
+  constexpr int P = fast_pts<R>(LOGM);  // points a thread
+  constexpr int T = M / P;
   constexpr int TW = fast_tw<R>(LOGM, OP);
 
   const int tid = threadIdx.x;
@@ -561,7 +601,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   if (soff >= 0) ioff = soff;
 
   // ---- load: v[r] = line p, element b + r T (stage-1 Stockham inputs) ----
-  Cx<R> v[8];
+  Cx<R> v[P];
   int emax = 0, emax_out = 0;
   if constexpr (IO::kDD) {
     if (!a.self_scale) {
@@ -573,47 +613,47 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     if (IO::kDD && IN_DD) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
       // exponents of the elements' first-pass lines, loaded ahead of the data
-      int tev[8];
+      int tev[P];
       if (IO::kDD && a.te_rescale) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) tev[r] = p < nvalid ? __ldg(a.te + te_index(a, o.tebase, t0 + p, b + r * T)) : emax;
+        for (int r = 0; r < P; ++r) tev[r] = p < nvalid ? __ldg(a.te + te_index(a, o.tebase, t0 + p, b + r * T)) : emax;
       }
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const float4 q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : make_float4(0.f, 0.f, 0.f, 0.f);
         v[r] = ld_dd4<R>(q);
       }
       if (IO::kDD && a.te_rescale) {
         bool off = false;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) off |= tev[r] != emax;
+        for (int r = 0; r < P; ++r) off |= tev[r] != emax;
         if (__any_sync(0xFFFFFFFFu, off)) {  // lines below the run exponent in this warp
 #pragma unroll
-          for (int r = 0; r < 8; ++r) v[r] = scale_pow2(v[r], pow2_le0(tev[r] - emax));
+          for (int r = 0; r < P; ++r) v[r] = scale_pow2(v[r], pow2_le0(tev[r] - emax));
         }
       }
     } else {
       // all loads first, conversions after: the conversion's rare-case
       // branch must not serialise the loads
       const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
-      MC raw[8];
+      MC raw[P];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) raw[r] = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
+      for (int r = 0; r < P; ++r) raw[r] = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
       if constexpr (IO::kDD) {
         if (a.self_scale) {
           unsigned emx = 0;
 #pragma unroll
-          for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
-          emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          for (int r = 0; r < P; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
+      for (int r = 0; r < P; ++r) v[r] = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
     }
     if (a.deriv == 1) {
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
         v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
       }
@@ -631,21 +671,21 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
         for (int t = 0; t < a.nterm; ++t) {
           const MC* in = reinterpret_cast<const MC*>(a.tsrc[t]) + ioff + (int64_t)p * sst;
 #pragma unroll
-          for (int r = 0; r < 8; ++r) {
+          for (int r = 0; r < P; ++r) {
             const MC q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
             emx = max(emx, max(dexp_u(q.x), dexp_u(q.y)));
           }
         }
-        emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+        emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
         emax_out = emax + a.emax_shift;
       }
     }
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = mk(R(0), R(0));
+    for (int r = 0; r < P; ++r) v[r] = mk(R(0), R(0));
     for (int t = 0; t < a.nterm; ++t) {
       const MC* in = reinterpret_cast<const MC*>(a.tsrc[t]) + ioff + (int64_t)p * sst;
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const MC q = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
         const int64_t idx = a.trole[t] == 0 ? (int64_t)(b + r * T) : a.trole[t] == 1 ? t0 + p : tidx[t];
         v[r] = v[r] + mul_ik(mk(mkr<R>(q.x, emax), mkr<R>(q.y, emax)), idx, a.thalf[t], a.tn[t],
@@ -658,7 +698,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     if (IO::kDD && IN_DD) {
       const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         int sg;
         const int k = x00_src(b + r * T, M, odd, sg);
         const float4 q = (p < nvalid && sg) ? in[(int64_t)k * ssa] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -668,10 +708,10 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       }
     } else {
       const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
-      MC raw[8];
-      int sgs[8];
+      MC raw[P];
+      int sgs[P];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const int k = x00_src(b + r * T, M, odd, sgs[r]);
         raw[r] = (p < nvalid && sgs[r]) ? in[(int64_t)k * ssa] : MC{0, 0};
       }
@@ -679,13 +719,13 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
         if (a.self_scale) {
           unsigned emx = 0;
 #pragma unroll
-          for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
-          emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          for (int r = 0; r < P; ++r) emx = max(emx, max(dexp_u(raw[r].x), dexp_u(raw[r].y)));
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const Cx<R> y = mk(mkr<R>(raw[r].x, emax), mkr<R>(raw[r].y, emax));
         v[r] = sgs[r] < 0 ? -y : y;
       }
@@ -695,10 +735,10 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     const int odd = a.r2r_odd;
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
-    MR ra[8], rb[8];
-    int sgs[8];
+    MR ra[P], rb[P];
+    int sgs[P];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = 0; r < P; ++r) {
       const int k = x00_src(b + r * T, M, odd, sgs[r]);
       const int64_t off = (int64_t)k * ssa;
       ra[r] = (i0 < nvalid && sgs[r]) ? in[off + (int64_t)i0 * sst] : MR(0);
@@ -708,22 +748,22 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       if (a.self_scale) {
         unsigned emx = 0;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
-        emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+        for (int r = 0; r < P; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
+        emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
         emax_out = emax + a.emax_shift;
       }
     }
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = 0; r < P; ++r) {
       const Cx<R> y = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
       v[r] = sgs[r] < 0 ? -y : y;
     }
   } else if constexpr (OP == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
-    MR ra[8], rb[8];
+    MR ra[P], rb[P];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = 0; r < P; ++r) {
       const int64_t off = (int64_t)(b + r * T) * ssa;
       ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MR(0);
       rb[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MR(0);
@@ -732,23 +772,23 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       if (a.self_scale) {
         unsigned emx = 0;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
-        emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+        for (int r = 0; r < P; ++r) emx = max(emx, max(dexp_u(ra[r]), dexp_u(rb[r])));
+        emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
         emax_out = emax + a.emax_shift;
       }
     }
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
+    for (int r = 0; r < P; ++r) v[r] = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
   } else {  // OP_C2R: Hermitian extension of two half spectra, n = M
     // m = n_in = M/2 + 1 (power-of-two M): the extension's case distinctions
     // are compile-time for every register but r = 0 and r = 4
     constexpr int m = M / 2 + 1;
     const int i0 = 2 * p, i1 = 2 * p + 1;
-    MC ra[8], rb[8];
+    MC ra[P], rb[P];
     if (!(IO::kDD && IN_DD)) {
       const MC* in = reinterpret_cast<const MC*>(src) + ioff;
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const int pos = b + r * T;
         const int64_t off = (int64_t)(pos < m ? pos : M - pos) * ssa;
         ra[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MC{0, 0};
@@ -758,15 +798,15 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
         if (a.self_scale) {
           unsigned emx = 0;
 #pragma unroll
-          for (int r = 0; r < 8; ++r)
+          for (int r = 0; r < P; ++r)
             emx = max(emx, max(max(dexp_u(ra[r].x), dexp_u(ra[r].y)), max(dexp_u(rb[r].x), dexp_u(rb[r].y))));
-          emax = line_exponent<R, LOGM, OP>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
           emax_out = emax + a.emax_shift;
         }
       }
     }
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = 0; r < P; ++r) {
       const int pos = b + r * T;
       const int k = pos < m ? pos : M - pos;
       const int64_t off = (int64_t)k * ssa;
@@ -797,12 +837,12 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   if (IO::kDD && a.self_scale && b == 0) lexp[p] = emax;
 
   // ---- stages ----
-  fast_stages<R, LOGM, SIGN, OP>(v, z, p, b, a.tw, a.lmap_tile != 0);
+  fast_stages<R, LOGM, SIGN, OP, P>(v, z, p, b, a.tw, a.lmap_tile != 0);
 
   // ---- store ----
   if (a.deriv == 2 && a.store_direct && OP == OP_C2C) {
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = 0; r < P; ++r) {
       const int64_t idx = a.deriv_role == 0 ? (int64_t)(b + r * T) : a.deriv_role == 1 ? t0 + p : didx;
       v[r] = mul_ik(v[r], idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
     }
@@ -811,7 +851,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
     // the split line's twiddles W_M^(n1 k2), k2 = b + r T, before any store
     const int64_t n1 = a.t4_role == 1 ? t0 + p : outer_index(a, (unsigned)bid, a.t4_role - 2);
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = tw_mul<R, SIGN>(v[r], a.t4_tab, (int)(n1 * (int64_t)(b + r * T)));
+    for (int r = 0; r < P; ++r) v[r] = tw_mul<R, SIGN>(v[r], a.t4_tab, (int)(n1 * (int64_t)(b + r * T)));
   }
   if (a.store_direct && OP != OP_R2C) {
     if constexpr (OP == OP_C2C || OP == OP_CSUM || OP == OP_C2CT) {
@@ -819,11 +859,11 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
         if (IO::kDD && OUT_DD) {
           float4* out = reinterpret_cast<float4*>(a.out) + ooff + (int64_t)p * a.out_st;
 #pragma unroll
-          for (int r = 0; r < 8; ++r) out[(int64_t)(b + r * T) * a.out_sa] = st_dd4(apply_scale(v[r], a));
+          for (int r = 0; r < P; ++r) out[(int64_t)(b + r * T) * a.out_sa] = st_dd4(apply_scale(v[r], a));
         } else {
           MC* out = reinterpret_cast<MC*>(a.out) + ooff + (int64_t)p * a.out_st;
 #pragma unroll
-          for (int r = 0; r < 8; ++r) {
+          for (int r = 0; r < P; ++r) {
             const Cx<R> y = apply_scale(v[r], a);
             MC o;
             o.x = outr<R>(y.re, emax_out);
@@ -837,7 +877,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       const int odd = a.r2r_odd, n = a.n_out;
       if (p < nvalid) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int r = 0; r < P; ++r) {
           const int k = b + r * T - odd;
           if (k < 0 || k >= n) continue;
           const Cx<R> y = apply_scale(x00_out(v[r], odd), a);
@@ -856,7 +896,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       MR* out = reinterpret_cast<MR*>(a.out) + ooff;
       const int i0 = 2 * p, i1 = 2 * p + 1;
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const int k = b + r * T - odd;
         if (k < 0 || k >= n) continue;
         const Cx<R> y = apply_scale(x00_out(v[r], odd), a);
@@ -868,7 +908,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       MR* out = reinterpret_cast<MR*>(a.out) + ooff;
       const int i0 = 2 * p, i1 = 2 * p + 1;
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < P; ++r) {
         const Cx<R> y = apply_scale(v[r], a);
         const int64_t off = (int64_t)(b + r * T) * a.out_sa;
         if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, emax_out);
@@ -882,7 +922,7 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   {
     Cx<R>* zw = z + sidx<R, LOGM, OP>(p, b);
 #pragma unroll
-    for (int r = 0; r < 8; ++r) zw[padded<R, LOGM>(r * T)] = v[r];
+    for (int r = 0; r < P; ++r) zw[padded<R, LOGM>(r * T)] = v[r];
   }
   __syncthreads();
   // the launch's thread count (fast_pass and fast_pass_tma launch
