@@ -184,8 +184,17 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
   }
 }
 
+// CTAs per SM the register allocation is sized for: two (64 registers for
+// the 512-thread Float32 CTAs, 128 for the 256-thread double-float ones).
+// Unbounded, the kernels take 80-100 (Float32) and 128-152 (dd) registers,
+// so one CTA per SM was resident; at two the spills are 0-12 bytes up to
+// L = 512 (Float32) and L = 2048 (dd), past which the bound is one.
+template <typename R>
+__host__ __device__ constexpr int bs_min_blocks(int logl) {
+  return sizeof(R) == 4 ? (logl <= 9 ? 2 : 1) : (logl <= 11 ? 2 : 1);
+}
 template <typename R, int LOGL, int OP>
-__global__ void __launch_bounds__(bs_threads<R>(LOGL)) bs_pass(const FastArgs a) {
+__global__ void __launch_bounds__(bs_threads<R>(LOGL), bs_min_blocks<R>(LOGL)) bs_pass(const FastArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   bs_tile<R, LOGL, OP>(a, blockIdx.x, reinterpret_cast<Cx<R>*>(smem_raw));
 }
