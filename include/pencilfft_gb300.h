@@ -217,6 +217,80 @@ int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* 
 int pfgb_batch_launch(pfgb_batch* batch, void* stream);
 int pfgb_batch_destroy(pfgb_batch* batch);
 
+/* One transform of pfgb_batch_create_ex: plan applied in `direction` (+1
+ * forward, -1 backward with `normalise` as in pfgb_backward) from src to dst;
+ * deriv_dim >= 0 fuses the spectral derivative along that (0-based) logical
+ * dimension of a domain of length deriv_length, as pfgb_forward_deriv (on the
+ * forward output) and pfgb_backward_deriv (on the backward input) do. */
+typedef struct pfgb_batch_op {
+  pfgb_plan* plan;
+  int32_t direction;
+  int32_t normalise;
+  void* dst;
+  const void* src;
+  int32_t deriv_dim;
+  int32_t reserved;
+  double deriv_length;
+} pfgb_batch_op;
+
+/* Forms of a batch.  GRAPH: the launches of every transform recorded into a
+ * CUDA graph, one branch per plan (pfgb_batch_create).  PERSISTENT: one
+ * launch of a persistent kernel (in a graph with the reset of its counters)
+ * that walks a device work list of every tile of every pass of every
+ * transform; its CTAs take tiles from a global counter in dependency order
+ * and wait, bounded, for the passes each tile depends on (the previous pass
+ * of its transform; for a transform's first pass, the last pass of every
+ * earlier transform on the same plan or with overlapping buffers).  The
+ * list is ordered by dependency level plus a rank that grows by one every
+ * 32 MB of data of the earlier transforms, so that the transforms in flight
+ * keep their data in L2 between passes.  Float32
+ * plans whose passes all have a tile form: c2c / r2c / c2r lines of 2 .. 1024
+ * points (powers of two up to 512 on the register tile, 3 * 2^k with
+ * 2^k = 128 .. 512 on the mixed-radix tile, the others on the Bluestein
+ * tile), with fused single derivatives; otherwise PFGB_ERR_UNSUPPORTED.
+ * AUTO: PERSISTENT where possible and the passes average at most 16 tiles
+ * (batches of many small fields, where the graph form is bound by launch
+ * latency), else GRAPH.  MEASURE: times the
+ * persistent form with waves of 8, 32 and 128 MB and in pure level order,
+ * and the graph form, at creation (launching the batch, which overwrites the
+ * destination arrays, and in-place sources, as FFTW's MEASURE planning does),
+ * and keeps the fastest. */
+#define PFGB_BATCH_GRAPH 0
+#define PFGB_BATCH_PERSISTENT 1
+#define PFGB_BATCH_AUTO 2
+#define PFGB_BATCH_MEASURE 3
+int pfgb_batch_create_ex(const pfgb_batch_op* ops, int n, int form, pfgb_batch** batch);
+
+/* The form a batch was recorded in, and for the persistent form its work
+ * list (passes, tiles), grid, dynamic shared memory per CTA and the wave size
+ * of the list's order (bytes; 0 for pure dependency-level order); graph_ms
+ * and persistent_ms are the times measured by PFGB_BATCH_MEASURE (the best
+ * persistent order; 0 otherwise). */
+typedef struct pfgb_batch_info {
+  int32_t form;
+  int32_t transforms;
+  int32_t items;
+  int32_t grid;
+  int64_t tiles;
+  int64_t smem;
+  double graph_ms;
+  double persistent_ms;
+  int64_t wave_bytes;
+} pfgb_batch_info;
+int pfgb_batch_get_info(pfgb_batch* batch, pfgb_batch_info* info);
+
+/* Device-side status of a persistent batch: synchronises `stream`, then
+ * returns in *flags, and clears, bit 8 if a dependency wait of the kernel gave
+ * up since the last call (every CTA then stopped taking tiles: the outputs of
+ * that launch are incomplete; later launches run normally).  0 for the graph
+ * form. */
+int pfgb_batch_status(pfgb_batch* batch, void* stream, int32_t* flags);
+
+/* Test hook for the give-up path of those waits: polls > 0 bounds every
+ * dependency wait of later launches at `polls` polls; 0 restores the default
+ * bound (of the order of a second).  PFGB_ERR_ARGUMENT for the graph form. */
+int pfgb_batch_set_wait_test(pfgb_batch* batch, int polls);
+
 /* Per-pass timing (replaces the reference's opt-in TimerOutputs sections
  * "PencilFFTs mul!", "FFT", ..., src/operations.jl:27,37,47,250,288,299).
  * When enabled, every kernel launch of the plan is bracketed by CUDA events

@@ -1,6 +1,7 @@
 // Bluestein (chirp-z) register pass: lines of any length M <= 2048 for c2c,
 // r2c and c2r, in FP32 or in double-float (doubles in and out, one exponent
-// per complex line), any input / output layout.
+// per complex line), any input / output layout; c2c lines take the fused
+// spectral derivative (i k times the input or the output).
 //
 // With w[j] = exp(s i pi j^2 / M) (s the transform's sign),
 //   X[k] = w[k] sum_n (x[n] w[n]) conj(w[k - n]),
@@ -57,7 +58,7 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
   if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
   const int lines = packed ? 2 * TW : TW;
   const TileOrigin o = tile_origin(a, (unsigned)bid, lines);
-  const int64_t t0 = o.t0, ooff = o.ooff, ioff = o.ioff;
+  const int64_t t0 = o.t0, ooff = o.ooff, ioff = o.ioff, didx = o.didx;
   const int nvalid = (int)min((int64_t)lines, a.nt - t0);
   const int ncl_valid = packed ? (nvalid + 1) / 2 : nvalid;
   const int64_t ssa = a.in_sa, sst = a.in_st;
@@ -108,6 +109,12 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
       if (pos >= m) { x.im = -x.im; B.im = -B.im; }
       x = mk(x.re - B.im, x.im + B.re);  // A + i B
     }
+    if constexpr (OP == OP_C2C) {
+      if (a.deriv == 1) {  // fused spectral derivative on the input
+        const int64_t idx = a.deriv_role == 0 ? (int64_t)pos : a.deriv_role == 1 ? t0 + p : didx;
+        x = mul_ik(x, idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
+      }
+    }
     v[r] = pos < M ? bs_mul(x, a.bs_chirp, pos) : mk(R(0), R(0));
   }
 
@@ -136,7 +143,11 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
       int i, k;
       if (a.out_tfast) { i = e % TW; k = e / TW; } else { i = (int)div31((unsigned)e, a.div_m); k = e - i * M; }
       if (i >= nvalid) continue;
-      const Cx<R> y = apply_scale(at(i, k), a);
+      Cx<R> y = apply_scale(at(i, k), a);
+      if (a.deriv == 2) {  // fused spectral derivative on the output
+        const int64_t idx = a.deriv_role == 0 ? (int64_t)k : a.deriv_role == 1 ? t0 + i : didx;
+        y = mul_ik(y, idx, a.deriv_half, a.deriv_n, a.k0_h, a.k0_l);
+      }
       MC q;
       q.x = outr<R>(y.re, eo(i));
       q.y = outr<R>(y.im, eo(i));

@@ -80,7 +80,9 @@ __device__ __forceinline__ void mr_dft_odd(Cx<R> (&v)[R0], const void* tw2, int 
   for (int i = 0; i < R0; ++i) v[i] = y[i];
 }
 
-template <typename R, int R0, int LOGN, int SIGN, int OP>
+// NT threads (mr_threads by default; the persistent batch kernel runs the
+// tile with its own CTA size), NT / (N / 8) complex lines a tile.
+template <typename R, int R0, int LOGN, int SIGN, int OP, int NT = mr_threads<R>(LOGN)>
 __device__ __forceinline__ void mr_tile(const FastArgs& a, int64_t bid, Cx<R>* z) {
   using IO = FastIO<R>;
   using MR = typename IO::MR;
@@ -88,8 +90,8 @@ __device__ __forceinline__ void mr_tile(const FastArgs& a, int64_t bid, Cx<R>* z
   constexpr int N = 1 << LOGN;
   constexpr int M = R0 * N;
   constexpr int T = N / 8;
-  constexpr int NT = mr_threads<R>(LOGN);
-  constexpr int TW = mr_tw<R>(LOGN);
+  constexpr int TW = NT / T;
+  static_assert(NT % T == 0 && TW >= 1, "mr_tile: threads must hold whole lines");
   constexpr int PITCH = mr_pitch<R, LOGN, OP>();
   constexpr bool packed = OP == OP_R2C || OP == OP_C2R;
 

@@ -29,6 +29,7 @@
 #include "pfgb_mr.cuh"
 #include "pfgb_bs.cuh"
 #include "pfgb_tc.cuh"
+#include "pfgb_persist.h"
 
 namespace pfgb {
 
@@ -592,6 +593,33 @@ static int prepare_core(pfgb_plan* P, Pass& ps, int M) {
   return PFGB_OK;
 }
 
+// The Bluestein register pass's form of a c2c / r2c / c2r pass of ps.M <= 2048
+// points: convolution length 2^logl >= 2 M - 1, its twiddles, the chirp and
+// filter tables, and the tile geometry.
+static int bluestein_form(pfgb_plan* P, Pass& ps) {
+  const int M = ps.M;
+  int logl = 4;
+  while ((1 << logl) < 2 * M - 1) ++logl;
+  std::vector<std::complex<ld>> w, bf;
+  bluestein_tables(M, 1 << logl, ps.sign, w, bf);
+  const std::string key = std::to_string(M) + "/" + std::to_string(1 << logl) + (ps.sign > 0 ? "+" : "-");
+  int rc = upload_fast_table(P, 1 << logl, &ps.ftw);
+  if (!rc) rc = upload_fast_vec(P, "bsw" + key, w, &ps.bs_chirp);
+  if (!rc) rc = upload_fast_vec(P, "bsf" + key, bf, &ps.bs_filt);
+  if (rc) return rc;
+  ps.mr = false;
+  ps.fast = false;
+  ps.bs = true;
+  ps.fop = ps.op;
+  ps.logl = logl;
+  const bool pk = fast_packed(ps.op);
+  ps.clines = P->rb == 8 ? bs_tw<dd>(logl) : bs_tw<float>(logl);
+  ps.lines = pk ? 2 * ps.clines : ps.clines;
+  ps.threads = P->rb == 8 ? bs_threads<dd>(logl) : bs_threads<float>(logl);
+  ps.smem = P->rb == 8 ? bs_smem<dd>(logl) : bs_smem<float>(logl);
+  return PFGB_OK;
+}
+
 static int prepare_pass(pfgb_plan* P, Pass& ps) {
   if (ps.pk == PK_COPY) {
     ps.threads = 256;
@@ -718,27 +746,11 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   // pass (double-float for Float64 data unless native FP64 was requested)
   if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R) && M >= 2 && M <= 2048 &&
       !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
-    int logl = 4;
-    while ((1 << logl) < 2 * M - 1) ++logl;
-    std::vector<std::complex<ld>> w, bf;
-    bluestein_tables(M, 1 << logl, ps.sign, w, bf);
-    const std::string key = std::to_string(M) + "/" + std::to_string(1 << logl) + (ps.sign > 0 ? "+" : "-");
-    int rc2 = upload_fast_table(P, 1 << logl, &ps.ftw);
-    if (!rc2) rc2 = upload_fast_vec(P, "bsw" + key, w, &ps.bs_chirp);
-    if (!rc2) rc2 = upload_fast_vec(P, "bsf" + key, bf, &ps.bs_filt);
-    if (rc2) return rc2;
     ps.g_lines = ps.lines;
     ps.g_clines = ps.clines;
     ps.g_threads = ps.threads;
     ps.g_smem = ps.smem;
-    ps.bs = true;
-    ps.fop = ps.op;
-    ps.logl = logl;
-    const bool pk = fast_packed(ps.op);
-    ps.clines = P->rb == 8 ? bs_tw<dd>(logl) : bs_tw<float>(logl);
-    ps.lines = pk ? 2 * ps.clines : ps.clines;
-    ps.threads = P->rb == 8 ? bs_threads<dd>(logl) : bs_threads<float>(logl);
-    ps.smem = P->rb == 8 ? bs_smem<dd>(logl) : bs_smem<float>(logl);
+    return bluestein_form(P, ps);
   }
   return PFGB_OK;
 }
@@ -1529,10 +1541,10 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       if (rc) return rc;
       rc = launch_mr(P, ps, F, grid, s);
       if (rc) return rc;
-    } else if (ps.bs && ps.variant != 2 && !(i == dpass && dv && dv->mode)) {
+    } else if (ps.bs && ps.variant != 2 && !(i == dpass && dv && dv->mode == 3)) {
       FastArgs F;
       int64_t grid = 0;
-      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, nullptr);
+      int rc = make_fast_args(P, ps, in, out, normalise && i == last_tr, F, grid, i == dpass ? dv : nullptr);
       if (rc) return rc;
       F.bs_m = ps.M;
       F.bs_chirp = ps.bs_chirp;
@@ -1542,8 +1554,8 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       if (rc) return rc;
     } else {
       // generic kernel (a Bluestein-eligible pass runs here with its generic
-      // geometry when a fused derivative applies to it, or when the planner
-      // measured this form faster)
+      // geometry when a fused sum of derivatives applies to it, or when the
+      // planner measured this form faster)
       const Pass g = ps.bs ? generic_form(ps) : ps;
       PassArgs A;
       int64_t grid = 0;
@@ -1560,6 +1572,83 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
   return PFGB_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// The passes of one execution as work items of the persistent batch kernel
+// (pfgb_persist.h) instead of launches.  Float32 plans; each pass takes the
+// tile form of its kernel: power-of-two lines of 8 .. 512 points the
+// register tile, 3 * 2^k lines (2^k = 128 .. 512) the mixed-radix tile with
+// the kernel's 512 threads, every other c2c / r2c / c2r line of 2 .. 1024
+// points the Bluestein tile (tables added to the plan when the pass ran
+// another kernel).  Other passes (copies, R2R, split lines, longer lines,
+// sums of derivatives) have no tile form: PFGB_ERR_UNSUPPORTED.
+// ---------------------------------------------------------------------------
+static int persist_opc(int op, int sign) { return op == OP_C2C ? (sign < 0 ? 0 : 1) : op == OP_R2C ? 2 : 3; }
+
+static int collect_persist(pfgb_plan* P, const Direction& dir, void* dst, const void* src, bool normalise,
+                           const Deriv* dv, std::vector<PersistItem>& items) {
+  if (P->rb != 4) return fail(PFGB_ERR_UNSUPPORTED, "persistent batch form: Float32 plans only");
+  const int m = (int)dir.passes.size();
+  int last_tr = -1, first_tr = -1;
+  for (int i = 0; i < m; ++i)
+    if (dir.passes[i].pk == PK_TRANSFORM) {
+      last_tr = i;
+      if (first_tr < 0) first_tr = i;
+    }
+  const int dpass = dv && dv->mode ? (dv->mode == 2 ? last_tr : first_tr) : -1;
+  if (dv && dv->mode == 3) return fail(PFGB_ERR_UNSUPPORTED, "persistent batch form: no sums of derivatives");
+  if (dv && dv->mode && (dpass < 0 || dir.passes[dpass].op != OP_C2C))
+    return fail(PFGB_ERR_UNSUPPORTED, "the fused derivative needs a complex-to-complex pass at that end of the plan");
+  for (int i = 0; i < m; ++i) {
+    const Pass& ps = dir.passes[i];
+    auto buf = [&](int b) -> void* {
+      switch (b) {
+        case 0: return const_cast<void*>(src);
+        case 1: return dst;
+        default: return P->scratch[b - 2];
+      }
+    };
+    const void* in = buf(ps.bin);
+    void* out = buf(ps.bout);
+    if (ps.pk == PK_COPY && in == out && ps.lin.same_order(ps.lout)) continue;
+    const bool cplx = ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R;
+    Pass q = ps;
+    int code = -1;
+    if (ps.pk == PK_TRANSFORM && cplx) {
+      if (ps.fast && !ps.tc && ps.fop == ps.op && ps.logm >= 3 && ps.logm <= 9) {
+        code = persist_code(PK_FAST_TILE, persist_opc(ps.op, ps.sign), ps.logm);
+      } else if (ps.mr && ps.r0 == 3 && ps.logn >= 7 && ps.logn <= 9) {
+        q.clines = kPersistThreads / ((1 << ps.logn) / 8);
+        q.lines = fast_packed(ps.op) ? 2 * q.clines : q.clines;
+        code = persist_code(PK_MR_TILE, persist_opc(ps.op, ps.sign), ps.logn);
+      } else if (!ps.fast && ps.M >= 2 && ps.M <= 1024) {
+        if (!ps.bs) {
+          int rc = bluestein_form(P, q);
+          if (rc) return rc;
+        }
+        code = persist_code(PK_BS_TILE, persist_opc(ps.op, ps.sign), q.logl);
+      }
+    }
+    if (code < 0 || persist_smem(code) == 0)
+      return fail(PFGB_ERR_UNSUPPORTED, "persistent batch form: pass " + std::to_string(i) + " has no tile form");
+    PersistItem it;
+    std::memset(&it, 0, sizeof(it));
+    int64_t grid = 0;
+    int rc = make_fast_args(P, q, in, out, normalise && i == last_tr, it.F, grid, i == dpass ? dv : nullptr);
+    if (rc) return rc;
+    if (q.bs) {
+      it.F.bs_m = q.M;
+      it.F.bs_chirp = q.bs_chirp;
+      it.F.bs_filt = q.bs_filt;
+      it.F.div_m = make_div31(q.op == OP_R2C ? q.M / 2 + 1 : q.M);
+    }
+    it.code = code;
+    it.ntiles = (int)grid;
+    if (it.ntiles > 0) items.push_back(it);
+  }
+  return PFGB_OK;
+}
+
 }  // namespace pfgb
 
 using namespace pfgb;
@@ -1567,6 +1656,448 @@ using namespace pfgb;
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Batches (pfgb_batch_*): graph form and persistent form
+// ---------------------------------------------------------------------------
+struct pfgb_batch {
+  cudaStream_t cap = nullptr;
+  std::vector<cudaStream_t> side;  // branches of the recorded graph form
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int n = 0;
+  int form = PFGB_BATCH_GRAPH;
+  int device = 0;
+  // persistent form: one device allocation holding the work list, the
+  // per-launch counters and the control words
+  void* dmem = nullptr;
+  int* status = nullptr;
+  int* polls = nullptr;
+  int items = 0;
+  int64_t tiles = 0;
+  int grid = 0;
+  size_t smem = 0;
+  int64_t wave = 0;  // data per wave of the work list's order (bytes)
+  double graph_ms = 0, persistent_ms = 0;
+};
+
+namespace pfgb {
+
+// one transform of a batch
+struct BatchOp {
+  pfgb_plan* plan;
+  int dir, norm;
+  void* dst;
+  const void* src;
+  bool has_dv;
+  Deriv dv;
+};
+
+static int run_op(const BatchOp& o, cudaStream_t s) {
+  pfgb_plan* P = o.plan;
+  const Deriv* d = o.has_dv ? &o.dv : nullptr;
+  return o.dir >= 0 ? execute(P, P->fwd, o.dst, o.src, s, false, 1, d)
+                    : execute(P, P->bwd, o.dst, o.src, s, o.norm != 0, -1, d);
+}
+
+// byte ranges read and written by an operation
+struct ByteRange {
+  const char* a;
+  int64_t n;
+};
+static bool ranges_overlap(const ByteRange& x, const ByteRange& y) { return x.a < y.a + y.n && y.a < x.a + x.n; }
+static void op_ranges(const BatchOp& o, ByteRange& rd, ByteRange& wr) {
+  const pfgb_plan* P = o.plan;
+  const bool f = o.dir >= 0;
+  const int64_t bi = P->inplace ? P->inplace_bytes : (f ? P->in_layout.bytes() : P->out_layout.bytes());
+  const int64_t bo = P->inplace ? P->inplace_bytes : (f ? P->out_layout.bytes() : P->in_layout.bytes());
+  rd = {static_cast<const char*>(o.src), bi};
+  wr = {static_cast<const char*>(o.dst), bo};
+}
+// operation j (earlier) must complete before operation i: the same plan
+// (shared scratch), or i reads or writes what j wrote, or writes what j read
+static bool op_depends(const std::vector<BatchOp>& ops, int i, int j) {
+  if (ops[i].plan == ops[j].plan) return true;
+  ByteRange ri, wi, rj, wj;
+  op_ranges(ops[i], ri, wi);
+  op_ranges(ops[j], rj, wj);
+  return ranges_overlap(wj, ri) || ranges_overlap(wj, wi) || ranges_overlap(rj, wi);
+}
+
+static void release_graph(pfgb_batch* B) {
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  B->exec = nullptr;
+  B->graph = nullptr;
+}
+
+static void release_batch(pfgb_batch* B) {
+  release_graph(B);
+  for (auto st : B->side) cudaStreamDestroy(st);
+  if (B->cap) cudaStreamDestroy(B->cap);
+  if (B->dmem) cudaFree(B->dmem);
+  delete B;
+}
+
+// Graph form: the launches of every transform recorded into one CUDA graph
+// with one branch per plan (the transforms of a plan share its scratch and
+// stay in order on their branch); a transform also waits for every earlier
+// one of another branch that it depends on (op_depends).
+static int record_graph_form(pfgb_batch* B, const std::vector<BatchOp>& ops) {
+  const int n = (int)ops.size();
+  std::vector<cudaEvent_t> events;
+  auto cleanup = [&](int rc) {
+    for (auto ev : events) cudaEventDestroy(ev);
+    return rc;
+  };
+  auto new_event = [&](cudaEvent_t* ev) {
+    cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) events.push_back(*ev);
+    return e;
+  };
+  std::vector<int> branch(n);
+  std::map<const pfgb_plan*, int> plan_branch;
+  for (int i = 0; i < n; ++i) {
+    auto it = plan_branch.find(ops[i].plan);
+    if (it == plan_branch.end()) {
+      cudaStream_t st = nullptr;
+      cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+      B->side.push_back(st);
+      it = plan_branch.emplace(ops[i].plan, (int)B->side.size() - 1).first;
+    }
+    branch[i] = it->second;
+  }
+  cudaError_t e = cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e)));
+  int rc = PFGB_OK;
+  cudaEvent_t fork = nullptr;
+  if ((e = new_event(&fork)) != cudaSuccess || (e = cudaEventRecord(fork, B->cap)) != cudaSuccess)
+    rc = fail(PFGB_ERR_CUDA, std::string("batch fork event: ") + cudaGetErrorString(e));
+  for (auto st : B->side)
+    if (!rc && (e = cudaStreamWaitEvent(st, fork, 0)) != cudaSuccess)
+      rc = fail(PFGB_ERR_CUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
+  std::vector<cudaEvent_t> done(n, nullptr);
+  for (int i = 0; i < n && !rc; ++i) {
+    cudaStream_t st = B->side[branch[i]];
+    for (int j = 0; j < i && !rc; ++j) {
+      if (branch[j] == branch[i] || !op_depends(ops, i, j)) continue;
+      if ((e = cudaStreamWaitEvent(st, done[j], 0)) != cudaSuccess)
+        rc = fail(PFGB_ERR_CUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
+    }
+    if (rc) break;
+    rc = run_op(ops[i], st);
+    if (!rc && ((e = new_event(&done[i])) != cudaSuccess || (e = cudaEventRecord(done[i], st)) != cudaSuccess))
+      rc = fail(PFGB_ERR_CUDA, std::string("batch event: ") + cudaGetErrorString(e));
+  }
+  // join every branch into the capturing stream
+  for (auto st : B->side) {
+    cudaEvent_t j = nullptr;
+    if ((e = new_event(&j)) != cudaSuccess || (e = cudaEventRecord(j, st)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(B->cap, j, 0)) != cudaSuccess) {
+      if (!rc) rc = fail(PFGB_ERR_CUDA, std::string("batch join: ") + cudaGetErrorString(e));
+    }
+  }
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(B->cap, &g);
+  B->graph = g;
+  if (rc) return cleanup(rc);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e)));
+  e = cudaGraphInstantiate(&B->exec, B->graph, 0);
+  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)));
+  return cleanup(PFGB_OK);
+}
+
+// default polls of a dependency wait of the persistent kernel (each poll an
+// acquire load and a 64 ns sleep: of the order of a second in all)
+constexpr int kPersistPolls = 1 << 21;
+
+// Persistent form: the work list of every transform's passes (collect_persist),
+// dependencies per pass, and a graph of one counter reset and one launch.
+// Items are ordered by level + rank, level the pass's dependency depth and
+// rank = (bytes read and written by the earlier transforms) / wave_bytes:
+// along a dependency the level grows and the rank does not fall, so every
+// item follows its dependencies, and the passes in flight at a time touch
+// about one wave of data per level (kept in L2 between the passes of a
+// transform) instead of every transform's (wave_bytes 0: level order).
+static int record_persistent_form(pfgb_batch* B, const std::vector<BatchOp>& ops, int64_t wave_bytes) {
+  const int n = (int)ops.size();
+  std::vector<PersistItem> items;
+  std::vector<std::vector<int>> deps;
+  std::vector<int> first(n), last(n);
+  for (int i = 0; i < n; ++i) {
+    const BatchOp& o = ops[i];
+    std::vector<PersistItem> mine;
+    const Direction& dir = o.dir >= 0 ? o.plan->fwd : o.plan->bwd;
+    int rc = collect_persist(o.plan, dir, o.dst, o.src, o.dir < 0 && o.norm != 0, o.has_dv ? &o.dv : nullptr, mine);
+    if (rc) return rc;
+    if (mine.empty()) return fail(PFGB_ERR_UNSUPPORTED, "persistent batch form: a transform without passes");
+    first[i] = (int)items.size();
+    for (size_t k = 0; k < mine.size(); ++k) {
+      std::vector<int> d;
+      if (k > 0) {
+        d.push_back((int)items.size() - 1);
+      } else {
+        for (int j = 0; j < i; ++j)
+          if (op_depends(ops, i, j)) d.push_back(last[j]);
+      }
+      items.push_back(mine[k]);
+      deps.push_back(d);
+    }
+    last[i] = (int)items.size() - 1;
+  }
+  const int m = (int)items.size();
+  std::vector<int64_t> key(m, 0);
+  {
+    std::vector<int64_t> rank(n, 0);
+    int64_t cum = 0;
+    for (int i = 0; i < n; ++i) {
+      rank[i] = wave_bytes > 0 ? cum / wave_bytes : 0;
+      ByteRange rd, wr;
+      op_ranges(ops[i], rd, wr);
+      cum += rd.n + wr.n;
+    }
+    std::vector<int64_t> level(m, 0);
+    for (int i = 0; i < n; ++i)
+      for (int x = first[i]; x <= last[i]; ++x) {
+        for (int d : deps[x]) level[x] = std::max(level[x], level[d] + 1);
+        key[x] = level[x] + rank[i];
+      }
+  }
+  std::vector<int> order(m);
+  for (int x = 0; x < m; ++x) order[x] = x;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+  std::vector<int> pos(m);
+  for (int x = 0; x < m; ++x) pos[order[x]] = x;
+  std::vector<PersistItem> sorted(m);
+  std::vector<int> dlist;
+  std::vector<long long> tb(m + 1, 0);
+  size_t smem = 0;
+  for (int x = 0; x < m; ++x) {
+    PersistItem it = items[order[x]];
+    it.dep_begin = (int)dlist.size();
+    for (int d : deps[order[x]]) dlist.push_back(pos[d]);
+    it.dep_end = (int)dlist.size();
+    sorted[x] = it;
+    tb[x + 1] = tb[x] + it.ntiles;
+    smem = std::max(smem, persist_smem(it.code));
+  }
+  int per_sm = 0;
+  int rc = persist_blocks_per_sm(smem, &per_sm);
+  if (rc) return rc;
+  if (per_sm < 1) return fail(PFGB_ERR_UNSUPPORTED, "persistent batch form: tiles do not fit on an SM");
+  int sms = 0;
+  PFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device));
+  // device layout: items | tile_begin | deps | next, abort, done[m] | status, polls
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t o_items = 0;
+  const size_t o_tb = o_items + al(sizeof(PersistItem) * m);
+  const size_t o_deps = o_tb + al(sizeof(long long) * (m + 1));
+  const size_t o_cnt = o_deps + al(sizeof(int) * std::max<size_t>(1, dlist.size()));
+  const size_t cnt_bytes = 16 + sizeof(unsigned) * m;
+  const size_t o_ctl = o_cnt + al(cnt_bytes);
+  const size_t total = o_ctl + 256;
+  PFGB_CUDA(cudaMalloc(&B->dmem, total));
+  char* base = static_cast<char*>(B->dmem);
+  PFGB_CUDA(cudaMemcpy(base + o_items, sorted.data(), sizeof(PersistItem) * m, cudaMemcpyHostToDevice));
+  PFGB_CUDA(cudaMemcpy(base + o_tb, tb.data(), sizeof(long long) * (m + 1), cudaMemcpyHostToDevice));
+  if (!dlist.empty())
+    PFGB_CUDA(cudaMemcpy(base + o_deps, dlist.data(), sizeof(int) * dlist.size(), cudaMemcpyHostToDevice));
+  const int ctl[2] = {0, kPersistPolls};
+  PFGB_CUDA(cudaMemcpy(base + o_ctl, ctl, sizeof(ctl), cudaMemcpyHostToDevice));
+  PersistArgs A;
+  A.items = reinterpret_cast<const PersistItem*>(base + o_items);
+  A.tile_begin = reinterpret_cast<const long long*>(base + o_tb);
+  A.deps = reinterpret_cast<const int*>(base + o_deps);
+  A.next = reinterpret_cast<unsigned long long*>(base + o_cnt);
+  A.abort_flag = reinterpret_cast<unsigned*>(base + o_cnt + 8);
+  A.done = reinterpret_cast<unsigned*>(base + o_cnt + 16);
+  A.status = reinterpret_cast<int*>(base + o_ctl);
+  A.polls = reinterpret_cast<const int*>(base + o_ctl + sizeof(int));
+  A.n = m;
+  A.total = tb[m];
+  B->status = A.status;
+  B->polls = reinterpret_cast<int*>(base + o_ctl + sizeof(int));
+  B->items = m;
+  B->tiles = tb[m];
+  B->grid = (int)std::min<long long>(tb[m], (long long)per_sm * sms);
+  B->smem = smem;
+  cudaError_t e = cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(PFGB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+  e = cudaMemsetAsync(base + o_cnt, 0, cnt_bytes, B->cap);
+  rc = e != cudaSuccess ? fail(PFGB_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e))
+                        : launch_persist(A, smem, B->grid, B->cap);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(B->cap, &g);
+  B->graph = g;
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(PFGB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&B->exec, B->graph, 0);
+  if (e != cudaSuccess) return fail(PFGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
+// ms per launch of an instantiated form (2 untimed launches, then 5 timed)
+static int time_form(pfgb_batch* B, double* ms) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  PFGB_CUDA(cudaEventCreate(&a));
+  cudaError_t e = cudaEventCreate(&b);
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaGraphLaunch(B->exec, B->cap);
+  if (e == cudaSuccess) e = cudaEventRecord(a, B->cap);
+  for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaGraphLaunch(B->exec, B->cap);
+  if (e == cudaSuccess) e = cudaEventRecord(b, B->cap);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float t = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (e != cudaSuccess) return fail(PFGB_ERR_CUDA, std::string("batch form timing: ") + cudaGetErrorString(e));
+  *ms = t / 5.0;
+  return PFGB_OK;
+}
+
+// Wave sizes of the persistent form: the default, and the candidates timed by
+// PFGB_BATCH_MEASURE (0: level order)
+constexpr int64_t kPersistWave = int64_t(32) << 20;
+constexpr int64_t kPersistWaveCandidates[] = {int64_t(8) << 20, int64_t(32) << 20, int64_t(128) << 20, 0};
+// PFGB_BATCH_AUTO takes the persistent form when a pass has at most this many
+// tiles on average (launch-bound batches).  Measured on GB300 with 64 Float32
+// r2c + c2r round trips per batch: fields of 8..24 points per axis (14 tiles
+// per pass) ran 0.34 ms persistent against 0.50 ms as a graph; from 32
+// points per axis (27-49 tiles per pass) the graph form was as fast or
+// faster between runs, and for 48..192 points (700) 4.8 against 6.5-6.7 ms:
+// the per-pass kernels read their arguments from the constant bank and run
+// the power-of-two and mixed-radix tiles at their own occupancy, while the
+// persistent kernel reads them from its work list and runs every tile at two
+// 512-thread CTAs per SM.
+constexpr int64_t kPersistAutoTilesPerPass = 16;
+
+// the persistent form's resources, moved out of / into a batch
+struct PersistForm {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void* dmem = nullptr;
+  int* status = nullptr;
+  int* polls = nullptr;
+  int items = 0, grid = 0;
+  int64_t tiles = 0, wave = 0;
+  size_t smem = 0;
+};
+static PersistForm take_persistent(pfgb_batch* B) {
+  PersistForm f;
+  f.graph = B->graph;
+  f.exec = B->exec;
+  f.dmem = B->dmem;
+  f.status = B->status;
+  f.polls = B->polls;
+  f.items = B->items;
+  f.grid = B->grid;
+  f.tiles = B->tiles;
+  f.wave = B->wave;
+  f.smem = B->smem;
+  B->graph = nullptr;
+  B->exec = nullptr;
+  B->dmem = nullptr;
+  B->status = B->polls = nullptr;
+  B->items = B->grid = 0;
+  B->tiles = B->wave = 0;
+  B->smem = 0;
+  return f;
+}
+static void put_persistent(pfgb_batch* B, const PersistForm& f) {
+  B->graph = f.graph;
+  B->exec = f.exec;
+  B->dmem = f.dmem;
+  B->status = f.status;
+  B->polls = f.polls;
+  B->items = f.items;
+  B->grid = f.grid;
+  B->tiles = f.tiles;
+  B->wave = f.wave;
+  B->smem = f.smem;
+}
+static void free_persistent(PersistForm& f) {
+  if (f.exec) cudaGraphExecDestroy(f.exec);
+  if (f.graph) cudaGraphDestroy(f.graph);
+  if (f.dmem) cudaFree(f.dmem);
+  f = PersistForm();
+}
+
+static int batch_create(const std::vector<BatchOp>& ops, int form, pfgb_batch** out) {
+  if (form < PFGB_BATCH_GRAPH || form > PFGB_BATCH_MEASURE) return fail(PFGB_ERR_ARGUMENT, "unknown batch form");
+  for (const BatchOp& o : ops)
+    if (o.plan->timing) return fail(PFGB_ERR_ARGUMENT, "disable plan timing before recording a batch");
+  pfgb_batch* B = new pfgb_batch();
+  B->n = (int)ops.size();
+  cudaGetDevice(&B->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    release_batch(B);
+    return fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  int rc = PFGB_OK;
+  if (form == PFGB_BATCH_GRAPH) {
+    rc = record_graph_form(B, ops);
+    B->form = PFGB_BATCH_GRAPH;
+  } else if (form != PFGB_BATCH_MEASURE) {
+    B->wave = kPersistWave;
+    rc = record_persistent_form(B, ops, B->wave);
+    B->form = PFGB_BATCH_PERSISTENT;
+    // AUTO: the persistent form where the batch is launch-bound (passes of a
+    // few tiles each), else the graph form (also for a pass without a tile
+    // form)
+    if (form == PFGB_BATCH_AUTO &&
+        (rc == PFGB_ERR_UNSUPPORTED || (!rc && B->tiles > kPersistAutoTilesPerPass * (int64_t)B->items))) {
+      PersistForm f = take_persistent(B);
+      free_persistent(f);
+      rc = record_graph_form(B, ops);
+      B->form = PFGB_BATCH_GRAPH;
+    }
+  } else {
+    // every wave size of the persistent form, then the graph form, timed on
+    // the batch's own buffers; the fastest is kept
+    PersistForm best;
+    double best_ms = -1;
+    for (int64_t w : kPersistWaveCandidates) {
+      B->wave = w;
+      rc = record_persistent_form(B, ops, w);
+      double ms = 0;
+      if (!rc) rc = time_form(B, &ms);
+      PersistForm f = take_persistent(B);
+      if (rc) {
+        free_persistent(f);
+        break;
+      }
+      if (best_ms < 0 || ms < best_ms) {
+        free_persistent(best);
+        best = f;
+        best_ms = ms;
+      } else {
+        free_persistent(f);
+      }
+    }
+    if (rc == PFGB_ERR_UNSUPPORTED && best_ms < 0) rc = PFGB_OK;  // graph form only
+    if (!rc) rc = record_graph_form(B, ops);
+    if (!rc) rc = time_form(B, &B->graph_ms);
+    B->persistent_ms = best_ms > 0 ? best_ms : 0;
+    B->form = PFGB_BATCH_GRAPH;
+    if (!rc && best_ms >= 0 && best_ms <= B->graph_ms) {
+      release_graph(B);
+      put_persistent(B, best);
+      B->form = PFGB_BATCH_PERSISTENT;
+    } else {
+      free_persistent(best);
+    }
+  }
+  if (rc) {
+    release_batch(B);
+    return rc;
+  }
+  *out = B;
+  return PFGB_OK;
+}
+
+}  // namespace pfgb
+
 extern "C" {
 
 const char* pfgb_version(void) { return "pencilfft_gb300 0.1.0 (sm_103a)"; }
@@ -2202,122 +2733,56 @@ int pfgb_backward(pfgb_plan* P, void* dst, const void* src, void* stream, int no
   return execute(P, P->bwd, dst, src, (cudaStream_t)stream, normalise != 0, -1);
 }
 
-struct pfgb_batch {
-  cudaStream_t cap = nullptr;
-  std::vector<cudaStream_t> side;  // branches of the recorded graph
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  int n = 0;
-};
+static int make_deriv(const pfgb_plan* P, int mode, int dim, double length, Deriv& dv);
 
-// Records the batch as a graph with one branch per plan (the transforms of a
-// plan share its scratch and stay in order on their branch); an operation
-// also waits for every earlier operation of another branch whose buffers it
-// reads or writes where that one wrote, or writes where that one read.
 int pfgb_batch_create(pfgb_plan* const* plans, const int* direction, const int* normalise,
                       void* const* dst, const void* const* src, int n, pfgb_batch** out) {
   g_last_error.clear();
   if (!out || n < 1 || !plans || !direction || !dst || !src)
     return fail(PFGB_ERR_ARGUMENT, "invalid batch description");
   *out = nullptr;
+  std::vector<BatchOp> ops(n);
   for (int i = 0; i < n; ++i) {
     if (!plans[i]) return fail(PFGB_ERR_ARGUMENT, "null plan in batch");
-    if (plans[i]->timing) return fail(PFGB_ERR_ARGUMENT, "disable plan timing before recording a batch");
     int rc = check_buffers(plans[i], dst[i], src[i], direction[i] >= 0);
     if (rc) return rc;
+    ops[i] = BatchOp{plans[i], direction[i], normalise ? normalise[i] : 0, dst[i], src[i], false, Deriv()};
   }
-  // byte ranges read and written by each operation
-  struct Range {
-    const char* a;
-    int64_t n;
-  };
-  std::vector<Range> rd(n), wr(n);
+  return batch_create(ops, PFGB_BATCH_GRAPH, out);
+}
+
+int pfgb_batch_create_ex(const pfgb_batch_op* desc, int n, int form, pfgb_batch** out) {
+  g_last_error.clear();
+  if (!out || n < 1 || !desc) return fail(PFGB_ERR_ARGUMENT, "invalid batch description");
+  *out = nullptr;
+  std::vector<BatchOp> ops(n);
   for (int i = 0; i < n; ++i) {
-    const pfgb_plan* P = plans[i];
-    const bool f = direction[i] >= 0;
-    const int64_t bi = P->inplace ? P->inplace_bytes : (f ? P->in_layout.bytes() : P->out_layout.bytes());
-    const int64_t bo = P->inplace ? P->inplace_bytes : (f ? P->out_layout.bytes() : P->in_layout.bytes());
-    rd[i] = {static_cast<const char*>(src[i]), bi};
-    wr[i] = {static_cast<const char*>(dst[i]), bo};
-  }
-  auto overlap = [](const Range& x, const Range& y) { return x.a < y.a + y.n && y.a < x.a + x.n; };
-  pfgb_batch* B = new pfgb_batch();
-  B->n = n;
-  std::vector<cudaEvent_t> events;
-  auto cleanup = [&](int rc) {
-    for (auto ev : events) cudaEventDestroy(ev);
-    if (rc) {
-      if (B->exec) cudaGraphExecDestroy(B->exec);
-      if (B->graph) cudaGraphDestroy(B->graph);
-      for (auto st : B->side) cudaStreamDestroy(st);
-      if (B->cap) cudaStreamDestroy(B->cap);
-      delete B;
-    }
-    return rc;
-  };
-  auto new_event = [&](cudaEvent_t* ev) {
-    cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) events.push_back(*ev);
-    return e;
-  };
-  cudaError_t e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking);
-  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
-  // one branch per distinct plan
-  std::vector<int> branch(n);
-  std::map<const pfgb_plan*, int> plan_branch;
-  for (int i = 0; i < n; ++i) {
-    auto it = plan_branch.find(plans[i]);
-    if (it == plan_branch.end()) {
-      cudaStream_t st = nullptr;
-      e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-      if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
-      B->side.push_back(st);
-      it = plan_branch.emplace(plans[i], (int)B->side.size() - 1).first;
-    }
-    branch[i] = it->second;
-  }
-  e = cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e)));
-  int rc = PFGB_OK;
-  cudaEvent_t fork = nullptr;
-  if ((e = new_event(&fork)) != cudaSuccess || (e = cudaEventRecord(fork, B->cap)) != cudaSuccess)
-    rc = fail(PFGB_ERR_CUDA, std::string("batch fork event: ") + cudaGetErrorString(e));
-  for (auto st : B->side)
-    if (!rc && (e = cudaStreamWaitEvent(st, fork, 0)) != cudaSuccess)
-      rc = fail(PFGB_ERR_CUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
-  std::vector<cudaEvent_t> done(n, nullptr);
-  for (int i = 0; i < n && !rc; ++i) {
-    pfgb_plan* P = plans[i];
-    cudaStream_t st = B->side[branch[i]];
-    for (int j = 0; j < i && !rc; ++j) {
-      if (branch[j] == branch[i]) continue;
-      if (overlap(wr[j], rd[i]) || overlap(wr[j], wr[i]) || overlap(rd[j], wr[i]))
-        if ((e = cudaStreamWaitEvent(st, done[j], 0)) != cudaSuccess)
-          rc = fail(PFGB_ERR_CUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
-    }
-    if (rc) break;
-    rc = direction[i] >= 0 ? execute(P, P->fwd, dst[i], src[i], st, false, 1)
-                           : execute(P, P->bwd, dst[i], src[i], st, normalise && normalise[i], -1);
-    if (!rc && ((e = new_event(&done[i])) != cudaSuccess || (e = cudaEventRecord(done[i], st)) != cudaSuccess))
-      rc = fail(PFGB_ERR_CUDA, std::string("batch event: ") + cudaGetErrorString(e));
-  }
-  // join every branch into the capturing stream
-  for (auto st : B->side) {
-    cudaEvent_t j = nullptr;
-    if ((e = new_event(&j)) != cudaSuccess || (e = cudaEventRecord(j, st)) != cudaSuccess ||
-        (e = cudaStreamWaitEvent(B->cap, j, 0)) != cudaSuccess) {
-      if (!rc) rc = fail(PFGB_ERR_CUDA, std::string("batch join: ") + cudaGetErrorString(e));
+    const pfgb_batch_op& d = desc[i];
+    if (!d.plan) return fail(PFGB_ERR_ARGUMENT, "null plan in batch");
+    int rc = check_buffers(d.plan, d.dst, d.src, d.direction >= 0);
+    if (rc) return rc;
+    ops[i] = BatchOp{d.plan, d.direction, d.normalise, d.dst, d.src, false, Deriv()};
+    if (d.deriv_dim >= 0) {
+      rc = make_deriv(d.plan, d.direction >= 0 ? 2 : 1, d.deriv_dim, d.deriv_length, ops[i].dv);
+      if (rc) return rc;
+      ops[i].has_dv = true;
     }
   }
-  cudaGraph_t g = nullptr;
-  e = cudaStreamEndCapture(B->cap, &g);
-  B->graph = g;
-  if (rc) return cleanup(rc);
-  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e)));
-  e = cudaGraphInstantiate(&B->exec, B->graph, 0);
-  if (e != cudaSuccess) return cleanup(fail(PFGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)));
-  cleanup(PFGB_OK);
-  *out = B;
+  return batch_create(ops, form, out);
+}
+
+int pfgb_batch_get_info(pfgb_batch* B, pfgb_batch_info* info) {
+  if (!B || !info) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  std::memset(info, 0, sizeof(*info));
+  info->form = B->form;
+  info->transforms = B->n;
+  info->items = B->items;
+  info->tiles = B->tiles;
+  info->grid = B->grid;
+  info->smem = (int64_t)B->smem;
+  info->graph_ms = B->graph_ms;
+  info->persistent_ms = B->persistent_ms;
+  info->wave_bytes = B->form == PFGB_BATCH_PERSISTENT ? B->wave : 0;
   return PFGB_OK;
 }
 
@@ -2328,13 +2793,31 @@ int pfgb_batch_launch(pfgb_batch* B, void* stream) {
   return PFGB_OK;
 }
 
+int pfgb_batch_status(pfgb_batch* B, void* stream, int32_t* flags) {
+  if (!B || !flags) return fail(PFGB_ERR_ARGUMENT, "null argument");
+  *flags = 0;
+  if (!B->status) return PFGB_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int word = 0;
+  PFGB_CUDA(cudaMemcpyAsync(&word, B->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PFGB_CUDA(cudaStreamSynchronize(s));
+  PFGB_CUDA(cudaMemsetAsync(B->status, 0, sizeof(int), s));
+  PFGB_CUDA(cudaStreamSynchronize(s));
+  *flags = word;
+  return PFGB_OK;
+}
+
+int pfgb_batch_set_wait_test(pfgb_batch* B, int polls) {
+  if (!B) return fail(PFGB_ERR_ARGUMENT, "null batch");
+  if (!B->polls) return fail(PFGB_ERR_ARGUMENT, "the batch is not in the persistent form");
+  const int v = polls > 0 ? polls : kPersistPolls;
+  PFGB_CUDA(cudaMemcpy(B->polls, &v, sizeof(int), cudaMemcpyHostToDevice));
+  return PFGB_OK;
+}
+
 int pfgb_batch_destroy(pfgb_batch* B) {
   if (!B) return PFGB_OK;
-  if (B->exec) cudaGraphExecDestroy(B->exec);
-  if (B->graph) cudaGraphDestroy(B->graph);
-  for (auto st : B->side) cudaStreamDestroy(st);
-  if (B->cap) cudaStreamDestroy(B->cap);
-  delete B;
+  release_batch(B);
   return PFGB_OK;
 }
 

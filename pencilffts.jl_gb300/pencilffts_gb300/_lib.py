@@ -72,6 +72,35 @@ class PassTiming(ctypes.Structure):
     ]
 
 
+class BatchOp(ctypes.Structure):
+    _fields_ = [
+        ("plan", ctypes.c_void_p),
+        ("direction", ctypes.c_int32),
+        ("normalise", ctypes.c_int32),
+        ("dst", ctypes.c_void_p),
+        ("src", ctypes.c_void_p),
+        ("deriv_dim", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("deriv_length", ctypes.c_double),
+    ]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("form", ctypes.c_int32),
+        ("transforms", ctypes.c_int32),
+        ("items", ctypes.c_int32),
+        ("grid", ctypes.c_int32),
+        ("tiles", ctypes.c_int64),
+        ("smem", ctypes.c_int64),
+        ("graph_ms", ctypes.c_double),
+        ("persistent_ms", ctypes.c_double),
+        ("wave_bytes", ctypes.c_int64),
+    ]
+
+
+BATCH_GRAPH, BATCH_PERSISTENT, BATCH_AUTO, BATCH_MEASURE = 0, 1, 2, 3
+
 # Every symbol the header declares, with (restype, argtypes).
 _vp = ctypes.c_void_p
 SIGNATURES = {
@@ -93,6 +122,11 @@ SIGNATURES = {
                                          ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_vp)]),
     "pfgb_batch_launch": (ctypes.c_int, [_vp, _vp]),
     "pfgb_batch_destroy": (ctypes.c_int, [_vp]),
+    "pfgb_batch_create_ex": (ctypes.c_int, [ctypes.POINTER(BatchOp), ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(_vp)]),
+    "pfgb_batch_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(BatchInfo)]),
+    "pfgb_batch_status": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(ctypes.c_int32)]),
+    "pfgb_batch_set_wait_test": (ctypes.c_int, [_vp, ctypes.c_int]),
     "pfgb_plan_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "pfgb_plan_get_timing": (ctypes.c_int, [_vp, ctypes.POINTER(PassTiming), ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_int)]),

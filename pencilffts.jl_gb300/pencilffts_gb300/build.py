@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "libpencilfft_gb300.so")
 INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["pfgb_plan.cu", "pfgb_kernels.cu", "pfgb_noalloc.cu", "pfgb_tc.cu"] + [
+SOURCES = ["pfgb_persist.cu", "pfgb_plan.cu", "pfgb_kernels.cu", "pfgb_noalloc.cu", "pfgb_tc.cu"] + [
     f"pfgb_fast_f32_{op}.cu" for op in ("c2c", "r2c", "c2r", "x00")] + [
     f"pfgb_fast_{t}_{op}_{iom}.cu" for t in ("dd", "fx")
     for op, ioms in (("c2c", (0, 1, 2, 3)), ("r2c", (0, 2)), ("c2r", (0, 1))) for iom in ioms] + [

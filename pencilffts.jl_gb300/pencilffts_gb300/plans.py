@@ -559,49 +559,107 @@ def _apply(dst, plan, src, forward, normalise, deriv=None):
 
 
 class Batch:
-    """Batched form: many transforms recorded once into a CUDA graph and
-    replayed with one launch (``pfgb_batch_create`` / ``pfgb_batch_launch``).
+    """Batched form: many transforms recorded once and replayed with one
+    launch (``pfgb_batch_create_ex`` / ``pfgb_batch_launch``).
 
-    ``ops`` is a sequence of ``(fn, dst, plan, src)`` with ``fn`` one of
-    ``mul_``, ``ldiv_``, ``bmul_``, exactly as the calls would be written; the
-    arrays are bound at construction and every ``launch()`` repeats all of the
-    recorded transforms on their current contents.
+    ``ops`` is a sequence of ``(fn, dst, plan, src)`` or
+    ``(fn, dst, plan, src, deriv)`` with ``fn`` one of ``mul_``, ``ldiv_``,
+    ``bmul_``, exactly as the calls would be written (``deriv=(dim, L)`` as
+    in ``mul_`` / ``ldiv_``); the arrays are bound at construction and every
+    ``launch()`` repeats all of the recorded transforms on their current
+    contents.
+
+    ``form``: ``"graph"`` records every transform's launches into one CUDA
+    graph with a branch per plan; ``"persistent"`` runs the whole batch as one
+    launch of a persistent kernel walking a work list of every tile of every
+    pass (Float32 plans whose passes all have a tile form; ``LibraryError``
+    otherwise); ``"auto"`` (default) takes the persistent form where
+    possible and the passes average at most 16 tiles (many small fields,
+    where the graph form is bound by launch latency), else the graph form;
+    ``"measure"`` times the persistent form in several work-list
+    orders and the graph form at construction, which runs the batch and so
+    overwrites the destination arrays as FFTW's MEASURE planning does, and
+    keeps the fastest.
     """
 
-    def __init__(self, ops):
+    FORMS = {"graph": _lib.BATCH_GRAPH, "persistent": _lib.BATCH_PERSISTENT, "auto": _lib.BATCH_AUTO,
+             "measure": _lib.BATCH_MEASURE}
+
+    def __init__(self, ops, form="auto"):
         ops = list(ops)
         if not ops:
             raise ArgumentError("empty batch")
+        if form not in self.FORMS:
+            raise ArgumentError(f"batch form must be one of {sorted(self.FORMS)}")
         n = len(ops)
-        plans = (ctypes.c_void_p * n)()
-        dirs = (ctypes.c_int * n)()
-        norms = (ctypes.c_int * n)()
-        dsts = (ctypes.c_void_p * n)()
-        srcs = (ctypes.c_void_p * n)()
+        desc = (_lib.BatchOp * n)()
         self._keep = []
-        for i, (fn, dst, plan, src) in enumerate(ops):
+        for i, op in enumerate(ops):
+            if len(op) == 4:
+                (fn, dst, plan, src), deriv = op, None
+            elif len(op) == 5:
+                fn, dst, plan, src, deriv = op
+            else:
+                raise ArgumentError("batch operations are (fn, dst, plan, src[, deriv])")
             if fn is mul_:
                 plan._check_arrays(src, dst)
-                dirs[i], norms[i] = 1, 0
+                direction, norm = 1, 0
             elif fn in (ldiv_, bmul_):
                 plan._check_arrays(dst, src)
-                dirs[i], norms[i] = -1, 1 if fn is ldiv_ else 0
+                direction, norm = -1, 1 if fn is ldiv_ else 0
             else:
                 raise ArgumentError("batch operations are mul_, ldiv_ or bmul_")
-            plans[i] = plan._handle.value
-            dsts[i] = dst.data_ptr()
-            srcs[i] = src.data_ptr()
+            d = desc[i]
+            d.plan = plan._handle.value
+            d.direction, d.normalise = direction, norm
+            d.dst, d.src = dst.data_ptr(), src.data_ptr()
+            d.deriv_dim, d.deriv_length = -1, 0.0
+            if deriv is not None:
+                dim, length = deriv
+                if not (1 <= int(dim) <= plan.ndims):
+                    raise ArgumentError(f"derivative dimension {dim} not in 1:{plan.ndims}")
+                d.deriv_dim, d.deriv_length = int(dim) - 1, float(length)
             self._keep.append((plan, dst, src))
         self._L = ops[0][2]._L
         h = ctypes.c_void_p()
-        _lib.check(self._L.pfgb_batch_create(plans, dirs, norms, dsts, srcs, n, ctypes.byref(h)),
-                   "pfgb_batch_create")
+        _lib.check(self._L.pfgb_batch_create_ex(desc, n, self.FORMS[form], ctypes.byref(h)),
+                   "pfgb_batch_create_ex")
         self._h = h
 
     def launch(self, stream=None):
         if stream is None:
             stream = _torch().cuda.current_stream().cuda_stream
         _lib.check(self._L.pfgb_batch_launch(self._h, ctypes.c_void_p(int(stream))), "pfgb_batch_launch")
+
+    def info(self) -> dict:
+        """The recorded form ("graph" or "persistent"), and for the persistent
+        form its work list (passes, tiles), grid, shared memory per CTA and
+        the wave size of the list's order; with ``form="measure"`` also the
+        measured times (graph form, best persistent order)."""
+        i = _lib.BatchInfo()
+        _lib.check(self._L.pfgb_batch_get_info(self._h, ctypes.byref(i)), "pfgb_batch_get_info")
+        return dict(form="persistent" if i.form == _lib.BATCH_PERSISTENT else "graph", transforms=i.transforms,
+                    items=i.items, tiles=i.tiles, grid=i.grid, smem=i.smem, wave_bytes=i.wave_bytes,
+                    graph_ms=i.graph_ms, persistent_ms=i.persistent_ms)
+
+    @property
+    def form(self) -> str:
+        return self.info()["form"]
+
+    def status(self, stream=None) -> int:
+        """Bits set by dependency waits of the persistent kernel that gave up
+        since the last call (8), cleared by the call; synchronises."""
+        if stream is None:
+            stream = _torch().cuda.current_stream().cuda_stream
+        f = ctypes.c_int32(0)
+        _lib.check(self._L.pfgb_batch_status(self._h, ctypes.c_void_p(int(stream)), ctypes.byref(f)),
+                   "pfgb_batch_status")
+        return f.value
+
+    def set_wait_test(self, polls: int) -> None:
+        """Test hook: bound every dependency wait of later launches at
+        ``polls`` polls (0 restores the default)."""
+        _lib.check(self._L.pfgb_batch_set_wait_test(self._h, int(polls)), "pfgb_batch_set_wait_test")
 
     def __del__(self):
         h = getattr(self, "_h", None)

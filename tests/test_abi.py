@@ -79,3 +79,35 @@ def test_julia_structs_mirror_the_header():
             assert ctypes.sizeof(jt) == ctypes.sizeof(ct) and getattr(jt, "_type_", jt) == getattr(ct, "_type_", ct), (jname, n)
     # offsets the binding relies on, e.g. scale_factor of pfgb_plan_info
     assert _lib.PlanInfo.scale_factor.offset == 184
+
+
+def test_struct_offsets_match_a_c_compiler(tmp_path):
+    """Every struct of the header, compiled by the host C compiler: size and
+    field offsets equal those of the ctypes mirrors."""
+    import shutil
+    import subprocess
+    import pytest
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"pfgb_plan_desc": _lib.PlanDesc, "pfgb_plan_info": _lib.PlanInfo,
+               "pfgb_pass_timing": _lib.PassTiming, "pfgb_batch_op": _lib.BatchOp,
+               "pfgb_batch_info": _lib.BatchInfo}
+    lines = ['#include <stdio.h>', '#include "pencilfft_gb300.h"', "int main(void) {"]
+    for cname, ct in mirrors.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in ct._fields_:  # (a trailing underscore avoids a Python keyword)
+            lines.append(f'  printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0].rstrip("_")}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    for cname, ct in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(ct), cname
+        for f in ct._fields_:
+            assert got[(cname, f[0])] == getattr(ct, f[0]).offset, (cname, f[0])

@@ -129,7 +129,8 @@ def test_batch_graph_replay(cuda):
     ws = [p.allocate_input() for p in plans]
     ops = [(P.mul_, v, p, u) for p, u, v in zip(plans, us, vs)]
     ops += [(P.ldiv_, w, p, v) for p, v, w in zip(plans, vs, ws)]
-    batch = P.Batch(ops)
+    batch = P.Batch(ops, form="graph")
+    assert batch.form == "graph"
     for trial in range(2):  # replay twice with new input contents
         xs = [rng.standard_normal(d).astype(np.float32) for d in sizes]
         for u, x in zip(us, xs):

@@ -190,11 +190,13 @@ def test_c5_vector_gradient_384(cuda):
     assert rel(div.to_logical(), ref) <= 2e-6
 
 
-def test_c5_batch_of_64_uneven(cuda):
+@pytest.mark.parametrize("form", ["graph", "persistent"])
+def test_c5_batch_of_64_uneven(cuda, form):
     """64 independent Float32 r2c + c2r round trips of sizes drawn from
     48..192 per axis (mixed radices, primes through Bluestein), recorded into
-    one batch (one CUDA graph, one branch per field) and launched once;
-    every field against the oracle."""
+    one batch (one CUDA graph with one branch per field, or one persistent
+    launch walking every tile of every pass) and launched once; every field
+    against the oracle."""
     import torch
     rng = np.random.default_rng(2024)
     sizes = [tuple(int(s) for s in rng.integers(48, 193, 3)) for _ in range(64)]
@@ -209,7 +211,8 @@ def test_c5_batch_of_64_uneven(cuda):
     ops = []
     for plan, (u, v, w) in zip(plans, arrays):
         ops += [(P.mul_, v, plan, u), (P.ldiv_, w, plan, v)]
-    batch = P.Batch(ops)
+    batch = P.Batch(ops, form=form)
+    assert batch.form == form
     batch.launch()
     torch.cuda.synchronize()
     for plan, (u, v, w), x, dims in zip(plans, arrays, xs, sizes):
