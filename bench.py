@@ -52,6 +52,9 @@ def parse():
                     help="other benchmark configurations to measure after the headline: "
                          "'all', 'none' or a comma list of C1,C2a,C2b,C3,C4,C5")
     ap.add_argument("--config-steps", type=int, default=10)
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="for ncu: build the 64 uneven Float32 fields of configuration C5, launch the batch "
+                         "once in the persistent form and once in the graph form, and exit")
     return ap.parse_args()
 
 
@@ -656,17 +659,17 @@ def config_c5(P, O, steps, warmup):
         arrs.append((u, v, w))
         ops += [(P.mul_, v, p, u), (P.ldiv_, w, p, v)]
     forms = {}
-    for f in ("graph", "persistent", "auto"):
+    for f in ("graph", "persistent", "measure"):
         b = P.Batch(ops, form=f)
         forms[f], _ = _timed(steps, warmup, b.launch)
-        if f == "auto":
-            auto_form = b.form
+        if f == "measure":
+            kept = b.form
         del b
     ms_seq_small, _ = _timed(steps, warmup, lambda: [(P.mul_(v, p, u), P.ldiv_(w, p, v))
                                                        for p, (u, v, w) in zip(plans, arrs)])
     out["small_fields_256"] = {
         "workload": "256 independent r2c + c2r round trips of 16^3 Float32 (launch-bound batch)",
-        "value": forms["auto"], "unit": "ms per 256 round trips", "form": auto_form,
+        "value": forms["measure"], "unit": "ms per 256 round trips", "form": kept,
         "graph_form_ms": forms["graph"], "persistent_form_ms": forms["persistent"],
         "sequential_ms": ms_seq_small}
     del plans, arrs, ops
@@ -932,6 +935,30 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profile_batch():
+    """The batch of configuration C5 (ii) in both forms, one launch each (the
+    persistent launch first), for a kernel profiler."""
+    import numpy as np
+    import torch
+
+    import pencilffts_gb300 as P
+    T = P.Transforms
+    rng = np.random.default_rng(2024)
+    sizes = [tuple(int(s) for s in rng.integers(48, 193, 3)) for _ in range(64)]
+    ops, keep = [], []
+    for d in sizes:
+        p = P.PencilFFTPlan(d, T.RFFT(), np.float32)
+        u, v, w = p.allocate_input(), p.allocate_output(), p.allocate_input()
+        u.copy_from_logical(rng.standard_normal(d).astype(np.float32))
+        keep.append((p, u, v, w))
+        ops += [(P.mul_, v, p, u), (P.ldiv_, w, p, v)]
+    forms = [P.Batch(ops, form="persistent"), P.Batch(ops, form="graph")]
+    for b in forms:
+        b.launch()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_batch": [b.info() for b in forms]}))
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -939,6 +966,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.profile_batch:
+        profile_batch()
         return
     if world > 1:
         import torch

@@ -64,10 +64,11 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
   const int64_t ssa = a.in_sa, sst = a.in_st;
   const int i0 = 2 * p, i1 = 2 * p + 1;
 
-  // ---- load (positions pos = b + r T < M of the line) ----
-  MC ra[8], rb[8];
+  // ---- load (positions pos = b + r T < M of the line; M <= L / 2 = 4 T,
+  // so r < 4) ----
+  MC ra[4], rb[4];
 #pragma unroll
-  for (int r = 0; r < 8; ++r) {
+  for (int r = 0; r < 4; ++r) {
     const int pos = b + r * T;
     ra[r] = MC{0, 0};
     rb[r] = MC{0, 0};
@@ -91,14 +92,16 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
   if constexpr (IO::kDD) {
     unsigned emx = 0;
 #pragma unroll
-    for (int r = 0; r < 8; ++r)
+    for (int r = 0; r < 4; ++r)
       emx = max(emx, max(max(dexp_u(ra[r].x), dexp_u(ra[r].y)), max(dexp_u(rb[r].x), dexp_u(rb[r].y))));
     emax = line_exponent<R, LOGL, OP_C2C>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
     if (b == 0) lexp[p] = emax;
   }
   Cx<R> v[8];
 #pragma unroll
-  for (int r = 0; r < 8; ++r) {
+  for (int r = 4; r < 8; ++r) v[r] = mk(R(0), R(0));  // zero padding (not read by the first stage)
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
     const int pos = b + r * T;
     Cx<R> x = mk(mkr<R>(ra[r].x, emax), mkr<R>(ra[r].y, emax));
     if constexpr (OP == OP_C2R) {
@@ -118,16 +121,18 @@ __device__ __forceinline__ void bs_tile(const FastArgs& a, int64_t bid, Cx<R>* z
     v[r] = pos < M ? bs_mul(x, a.bs_chirp, pos) : mk(R(0), R(0));
   }
 
-  // ---- convolution: forward L-point transform, filter, inverse ----
-  fast_stages<R, LOGL, -1, OP_C2C>(v, z, p, b, a.tw, a.lmap_tile != 0);
+  // ---- convolution: forward L-point transform (its inputs' upper half is
+  // the zero padding), filter, inverse ----
+  fast_stages<R, LOGL, -1, OP_C2C, 8, true>(v, z, p, b, a.tw, a.lmap_tile != 0);
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = bs_mul(v[r], a.bs_filt, b + r * T);
   fast_stages<R, LOGL, 1, OP_C2C>(v, z, p, b, a.tw, a.lmap_tile != 0);
 
-  // ---- X[k] = w[k] c[k], k < M, into the line's shared memory ----
+  // ---- X[k] = w[k] c[k], k < M <= 4 T, into the line's shared memory (the
+  // inverse transform's outputs at r >= 4 are not used) ----
   // (fast_stages ends after a barrier that follows its last exchange read)
 #pragma unroll
-  for (int r = 0; r < 8; ++r) {
+  for (int r = 0; r < 4; ++r) {
     const int pos = b + r * T;
     if (pos < M) z[sidx<R, LOGL, OP_C2C>(p, pos)] = bs_mul(v[r], a.bs_chirp, pos);
   }

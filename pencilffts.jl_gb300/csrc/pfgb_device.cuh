@@ -218,6 +218,34 @@ __device__ __forceinline__ void dft8(Cx<R>* v) {
   for (int i = 0; i < 8; ++i) v[i] = y[i];
 }
 
+// dft4 / dft8 of inputs whose upper half is zero (x2 = x3 = 0; v[4..7] = 0),
+// which are not read: the first stage of a zero-padded transform
+template <int SIGN, typename R>
+__device__ __forceinline__ void dft4_zh(Cx<R>& x0, Cx<R>& x1, Cx<R>& x2, Cx<R>& x3) {
+  const Cx<R> a = x0, t3 = mul_w4<SIGN>(x1);
+  x0 = a + x1;
+  x2 = a - x1;
+  x3 = a - t3;
+  x1 = a + t3;
+}
+template <int SIGN, typename R>
+__device__ __forceinline__ void dft8_zh(Cx<R>* v) {
+  dft4_zh<SIGN>(v[0], v[2], v[4], v[6]);
+  dft4_zh<SIGN>(v[1], v[3], v[5], v[7]);
+  v[3] = w16mul<SIGN, 2>(v[3]);
+  v[5] = w16mul<SIGN, 4>(v[5]);
+  v[7] = w16mul<SIGN, 6>(v[7]);
+  Cx<R> y[8];
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) {
+    Cx<R> a0 = v[2 * k2], a1 = v[2 * k2 + 1];
+    y[k2] = a0 + a1;
+    y[k2 + 4] = a0 - a1;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = y[i];
+}
+
 template <int SIGN, typename R>
 __device__ __forceinline__ void dft16(Cx<R>* v) {
   // n = n1 + 4 n2, k = k2 + 4 k1; a[n1][k2] lives in v[n1 + 4 k2]

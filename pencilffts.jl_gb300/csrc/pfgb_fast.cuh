@@ -307,10 +307,12 @@ __device__ __forceinline__ void line_sync(bool lanes_across_lines, int p) {
 // The register stages of a line of M = 2^LOGM points, P points a thread
 // (positions b + r M/P): radix-P stages (dft8 or dft16), then one radix-2,
 // 4 or 8 stage when log2 M is not a multiple of log2 P; outputs left in
-// natural order at the same positions.
-template <typename R, int LOGM, int SIGN, int OP, int P = 8>
+// natural order at the same positions.  ZH: the inputs at positions M/2 and
+// above are zero (v[4..7] with P = 8) and are not read.
+template <typename R, int LOGM, int SIGN, int OP, int P = 8, bool ZH = false>
 __device__ __forceinline__ void fast_stages(Cx<R> (&v)[P], Cx<R>* z, int p, int b, const void* tw,
                                             bool lanes_across_lines) {
+  static_assert(!ZH || P == 8, "zero upper half: 8 points a thread");
   constexpr int M = 1 << LOGM;
   constexpr int T = M / P;
   constexpr int LP = P == 16 ? 4 : 3;
@@ -329,6 +331,7 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[P], Cx<R>* z, int p, int 
         for (int r = 1; r < P; ++r) v[r] = tw_mul<R, SIGN>(v[r], tw, r * step);
       }
       if constexpr (P == 16) dft16<SIGN>(v);
+      else if (ZH && s == 0) dft8_zh<SIGN>(v);
       else dft8<SIGN>(v);
       if (!last) {
         Cx<R>* zw = z + sidx<R, LOGM, OP>(p, (b - j) * P + j);

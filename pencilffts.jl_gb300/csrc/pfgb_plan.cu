@@ -1959,17 +1959,7 @@ static int time_form(pfgb_batch* B, double* ms) {
 // PFGB_BATCH_MEASURE (0: level order)
 constexpr int64_t kPersistWave = int64_t(32) << 20;
 constexpr int64_t kPersistWaveCandidates[] = {int64_t(8) << 20, int64_t(32) << 20, int64_t(128) << 20, 0};
-// PFGB_BATCH_AUTO takes the persistent form when a pass has at most this many
-// tiles on average (launch-bound batches).  Measured on GB300 with 64 Float32
-// r2c + c2r round trips per batch: fields of 8..24 points per axis (14 tiles
-// per pass) ran 0.34 ms persistent against 0.50 ms as a graph; from 32
-// points per axis (27-49 tiles per pass) the graph form was as fast or
-// faster between runs, and for 48..192 points (700) 4.8 against 6.5-6.7 ms:
-// the per-pass kernels read their arguments from the constant bank and run
-// the power-of-two and mixed-radix tiles at their own occupancy, while the
-// persistent kernel reads them from its work list and runs every tile at two
-// 512-thread CTAs per SM.
-constexpr int64_t kPersistAutoTilesPerPass = 16;
+
 
 // the persistent form's resources, moved out of / into a batch
 struct PersistForm {
@@ -2042,11 +2032,8 @@ static int batch_create(const std::vector<BatchOp>& ops, int form, pfgb_batch** 
     B->wave = kPersistWave;
     rc = record_persistent_form(B, ops, B->wave);
     B->form = PFGB_BATCH_PERSISTENT;
-    // AUTO: the persistent form where the batch is launch-bound (passes of a
-    // few tiles each), else the graph form (also for a pass without a tile
-    // form)
-    if (form == PFGB_BATCH_AUTO &&
-        (rc == PFGB_ERR_UNSUPPORTED || (!rc && B->tiles > kPersistAutoTilesPerPass * (int64_t)B->items))) {
+    // AUTO: a pass without a tile form leaves the batch to the graph form
+    if (form == PFGB_BATCH_AUTO && rc == PFGB_ERR_UNSUPPORTED) {
       PersistForm f = take_persistent(B);
       free_persistent(f);
       rc = record_graph_form(B, ops);

@@ -569,14 +569,12 @@ class Batch:
     ``launch()`` repeats all of the recorded transforms on their current
     contents.
 
-    ``form``: ``"graph"`` records every transform's launches into one CUDA
-    graph with a branch per plan; ``"persistent"`` runs the whole batch as one
+    ``form``: ``"graph"`` (default) records every transform's launches into
+    one CUDA graph with a branch per plan; ``"persistent"`` runs the whole batch as one
     launch of a persistent kernel walking a work list of every tile of every
     pass (Float32 plans whose passes all have a tile form; ``LibraryError``
-    otherwise); ``"auto"`` (default) takes the persistent form where
-    possible and the passes average at most 16 tiles (many small fields,
-    where the graph form is bound by launch latency), else the graph form;
-    ``"measure"`` times the persistent form in several work-list
+    otherwise); ``"auto"`` takes the persistent form where possible, else
+    the graph form; ``"measure"`` times the persistent form in several work-list
     orders and the graph form at construction, which runs the batch and so
     overwrites the destination arrays as FFTW's MEASURE planning does, and
     keeps the fastest.
@@ -585,7 +583,7 @@ class Batch:
     FORMS = {"graph": _lib.BATCH_GRAPH, "persistent": _lib.BATCH_PERSISTENT, "auto": _lib.BATCH_AUTO,
              "measure": _lib.BATCH_MEASURE}
 
-    def __init__(self, ops, form="auto"):
+    def __init__(self, ops, form="graph"):
         ops = list(ops)
         if not ops:
             raise ArgumentError("empty batch")

@@ -211,16 +211,15 @@ def test_measured_form(cuda):
         assert rel(w.to_logical(), x) <= TOL
 
 
-def test_auto_form_follows_tiles_per_pass(cuda):
-    """form="auto": many small fields (a few tiles per pass, launch-bound)
-    take the persistent form, large fields the graph form."""
-    small = _round_trips([(12, 20, 16)] * 6 + [(24, 9, 30)] * 6, "auto", seed=1)
-    assert small[4].form == "persistent"
-    large = _round_trips([(128, 96, 80)], "auto", seed=1)
-    assert large[4].form == "graph"
-    for plans, xs, vs, ws, batch in (small, large):
-        batch.launch()
-        _sync()
-        for p, x, v, w in zip(plans, xs, vs, ws):
-            assert rel(v.to_logical(), oracle_plan(p).forward(x)) <= TOL
-            assert rel(w.to_logical(), x) <= TOL
+def test_auto_form(cuda):
+    """form="auto" records the persistent form when every pass has a tile
+    form; the default form is the graph form."""
+    plans, xs, vs, ws, batch = _round_trips([(12, 20, 16), (24, 9, 30)], "auto", seed=1)
+    assert batch.form == "persistent"
+    batch.launch()
+    _sync()
+    for p, x, v, w in zip(plans, xs, vs, ws):
+        assert rel(v.to_logical(), oracle_plan(p).forward(x)) <= TOL
+        assert rel(w.to_logical(), x) <= TOL
+    p = plans[0]
+    assert P.Batch([(P.mul_, vs[0], p, p.allocate_input())]).form == "graph"
