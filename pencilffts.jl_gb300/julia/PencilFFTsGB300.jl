@@ -20,7 +20,12 @@ reversed when `permute_dims = Val(true)`):
   `ManyPencilArray`);
 - `scale_factor`, `size`, `is_inplace`, `eltype_input`, `eltype_output`;
 - the fused spectral operators of the library: `ldiv_deriv!` (one i k
-  multiply), `ldiv_divergence!` and `ldiv_curl!` (test/include/FourierOperations.jl).
+  multiply), `ldiv_divergence!` and `ldiv_curl!` (test/include/FourierOperations.jl);
+- batches: `GB300Batch([(mul!, vF, p, u), (ldiv!, du, p, vF, (dim, L)), ...];
+  form = :graph)` records many transforms (any plans and sizes, optional fused
+  derivative) for one `launch(batch)` (the collections of
+  src/operations.jl:129-152 as one launch): `:graph` one CUDA graph with a
+  branch per plan, `:persistent` one work-list kernel, `:auto`, `:measure`.
 
 The transforms are the reference's own `Transforms` types; the mapping to the
 C ABI codes is `abi_kind`.
@@ -285,5 +290,50 @@ function ldiv_curl!(ω, p::GB300Plan{T,3}, uF, L) where {T}
     end
     ω
 end
+
+# pfgb_batch_op (include/pencilfft_gb300.h)
+struct BatchOp
+    plan::Ptr{Cvoid}
+    direction::Int32
+    normalise::Int32
+    dst::Ptr{Cvoid}
+    src::Ptr{Cvoid}
+    deriv_dim::Int32
+    reserved::Int32
+    deriv_length::Float64
+end
+
+const BATCH_FORMS = Dict(:graph => 0, :persistent => 1, :auto => 2, :measure => 3)
+
+mutable struct GB300Batch
+    handle::Ptr{Cvoid}
+    keep::Vector{Any}  # the plans and arrays the recorded launches use
+end
+
+# ops: (mul!, dst, p, src), (ldiv!, dst, p, src) or (bmul!, dst, p, src), each
+# optionally followed by (dim, L) for a fused spectral derivative (1-based dim)
+function GB300Batch(ops::AbstractVector; form::Symbol = :graph)
+    descs = BatchOp[]
+    for op in ops
+        f, dst, p, src = op[1], op[2], op[3], op[4]
+        dir, norm = f === LinearAlgebra.mul! ? (1, 0) : f === LinearAlgebra.ldiv! ? (-1, 1) :
+                    f === bmul! ? (-1, 0) : throw(ArgumentError("batch operations are mul!, ldiv! or bmul!"))
+        dd, dl = length(op) >= 5 ? (Int32(op[5][1] - 1), Float64(op[5][2])) : (Int32(-1), 0.0)
+        push!(descs, BatchOp(p.handle, dir, norm, Ptr{Cvoid}(UInt(pointer(dst))), Ptr{Cvoid}(UInt(pointer(src))),
+                             dd, 0, dl))
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:pfgb_batch_create_ex, LIB), Cint, (Ptr{BatchOp}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                descs, length(descs), BATCH_FORMS[form], h))
+    b = GB300Batch(h[], collect(Any, ops))
+    finalizer(b) do x
+        x.handle == C_NULL || ccall((:pfgb_batch_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle)
+        x.handle = C_NULL
+    end
+    b
+end
+
+launch(b::GB300Batch) =
+    (check(ccall((:pfgb_batch_launch, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), b.handle, stream_ptr())); b)
 
 end # module

@@ -57,7 +57,8 @@ def _julia_struct(name):
     src = open(os.path.join(REPO, "pencilffts.jl_gb300", "julia", "PencilFFTsGB300.jl")).read()
     m = re.search(r"^struct %s\n(.*?)^end" % name, src, flags=re.S | re.M)
     assert m, name
-    scalar = {"Int32": ctypes.c_int32, "Int64": ctypes.c_int64, "Float64": ctypes.c_double}
+    scalar = {"Int32": ctypes.c_int32, "Int64": ctypes.c_int64, "Float64": ctypes.c_double,
+              "Ptr{Cvoid}": ctypes.c_void_p}
     consts = {"MAX_DIMS": _lib.MAX_DIMS, "MAX_EXTRA": 4}
     out = []
     for line in m.group(1).strip().splitlines():
@@ -68,10 +69,10 @@ def _julia_struct(name):
 
 
 def test_julia_structs_mirror_the_header():
-    """The Julia binding's PlanDesc and PlanInfo have the C structs' fields, in
+    """The Julia binding's PlanDesc, PlanInfo and BatchOp have the C structs' fields, in
     order and with the same types (Julia lays isbits structs out with C
     alignment), so ccall passes them by reference unchanged."""
-    for jname, cstruct in (("PlanDesc", _lib.PlanDesc), ("PlanInfo", _lib.PlanInfo)):
+    for jname, cstruct in (("PlanDesc", _lib.PlanDesc), ("PlanInfo", _lib.PlanInfo), ("BatchOp", _lib.BatchOp)):
         jf = _julia_struct(jname)
         cf = cstruct._fields_
         assert [n for n, _ in jf] == [n for n, _ in cf], jname
