@@ -191,8 +191,6 @@ __global__ void __launch_bounds__(kPersistThreads, 2) persist_batch(const Persis
   }
 }
 
-static_assert(sizeof(FastArgs) % sizeof(int) == 0, "FastArgs copy by words");
-
 size_t persist_smem(int code) {
   const int lg = code % 16, opc = (code / 16) % 4, kind = code / 64;
   const int op = opc < 2 ? OP_C2C : opc == 2 ? OP_R2C : OP_C2R;

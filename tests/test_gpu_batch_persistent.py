@@ -223,3 +223,45 @@ def test_auto_form(cuda):
         assert rel(w.to_logical(), x) <= TOL
     p = plans[0]
     assert P.Batch([(P.mul_, vs[0], p, p.allocate_input())]).form == "graph"
+
+
+def test_single_transform_and_inplace_plans(cuda):
+    """A batch of one transform, and an in-place FFT! plan's forward and
+    backward on one ManyPencilArray (reference test/transforms.jl:177-256),
+    each in the forms it records under "auto"; results against the oracle."""
+    plan = P.PencilFFTPlan((24, 20, 9), T.RFFT(), F32)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((24, 20, 9)).astype(F32)
+    u, v = input_array(plan, x), plan.allocate_output()
+    one = P.Batch([(P.mul_, v, plan, u)], form="persistent")
+    one.launch()
+    _sync()
+    assert rel(v.to_logical(), oracle_plan(plan).forward(x)) <= TOL
+
+    ip = P.PencilFFTPlan((16, 12, 6), T.FFT_(), F32)
+    vi = ip.allocate_input()
+    xi = (rng.standard_normal((16, 12, 6)) + 1j * rng.standard_normal((16, 12, 6))).astype(np.complex64)
+    vi.first().copy_from_logical(xi)
+    b = P.Batch([(P.mul_, vi, ip, vi), (P.ldiv_, vi, ip, vi)], form="auto")
+    assert b.form in ("graph", "persistent")
+    b.launch()
+    _sync()
+    assert rel(vi.first().to_logical(), xi) <= TOL
+    f = P.Batch([(P.mul_, vi, ip, vi)], form="auto")
+    vi.first().copy_from_logical(xi)
+    f.launch()
+    _sync()
+    assert rel(vi.last().to_logical(), oracle_plan(ip).forward(xi)) <= TOL
+
+
+def test_empty_and_malformed_batches(cuda):
+    plan = P.PencilFFTPlan((8, 8, 8), T.RFFT(), F32)
+    u, v = plan.allocate_input(), plan.allocate_output()
+    with pytest.raises(P.ArgumentError):
+        P.Batch([])
+    with pytest.raises(P.ArgumentError):
+        P.Batch([(P.mul_, v, plan, u)], form="fastest")
+    with pytest.raises(P.ArgumentError):
+        P.Batch([(P.mul_, v, plan)])
+    with pytest.raises(P.ArgumentError):
+        P.Batch([(P.ldiv_, u, plan, v, (4, 1.0))])
