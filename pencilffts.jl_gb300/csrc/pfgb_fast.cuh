@@ -202,10 +202,15 @@ __host__ __device__ constexpr int fast_pitch_extra(int tw, int ebytes) {
   return ebytes == 16 ? (tw >= 8 ? 1 : tw == 4 ? 2 : tw == 2 ? 4 : 0)
                       : (tw >= 16 ? 1 : tw == 8 ? 2 : tw == 4 ? 4 : tw == 2 ? 8 : 0);
 }
+// bytes of one element of the exchange layout
+template <typename R>
+__host__ __device__ constexpr int fast_xbytes() {
+  return (int)sizeof(Cx<R>);
+}
 template <typename R>
 __host__ __device__ constexpr int fast_pitch(int logm, int op = OP_C2C) {
-  return (1 << logm) + ((1 << logm) >> fast_pad_shift(logm, (int)sizeof(Cx<R>))) +
-         fast_pitch_extra(fast_tw<R>(logm, op), (int)sizeof(Cx<R>));
+  return (1 << logm) + ((1 << logm) >> fast_pad_shift(logm, fast_xbytes<R>())) +
+         fast_pitch_extra(fast_tw<R>(logm, op), fast_xbytes<R>());
 }
 template <typename R>
 __host__ __device__ constexpr size_t fast_smem(int logm, int op = OP_C2C) {
@@ -274,11 +279,20 @@ __device__ __forceinline__ Cx<R> tw_mul(Cx<R> v, const void* tw, int m) {
 // conflicts for the strided stage writes and the across-line accesses).
 template <typename R, int LOGM>
 __host__ __device__ constexpr int padded(int pos) {
-  return pos + (pos >> fast_pad_shift(LOGM, (int)sizeof(Cx<R>)));
+  return pos + (pos >> fast_pad_shift(LOGM, fast_xbytes<R>()));
 }
 template <typename R, int LOGM, int OP>
 __device__ __forceinline__ int sidx(int p, int pos) {
   return p * fast_pitch<R>(LOGM, OP) + padded<R, LOGM>(pos);
+}
+// Exchange element i of a tile's shared-memory buffer z.
+template <typename R, int LOGM, int OP>
+__device__ __forceinline__ void xst(Cx<R>* z, int i, const Cx<R>& v) {
+  z[i] = v;
+}
+template <typename R, int LOGM, int OP>
+__device__ __forceinline__ Cx<R> xld(const Cx<R>* z, int i) {
+  return z[i];
 }
 // The padding is additive over the exchange patterns: with all sizes powers
 // of two, padded(p0 + r L) = padded(p0) + padded(r L) for 0 <= r < 8 when
@@ -334,9 +348,9 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[P], Cx<R>* z, int p, int 
       else if (ZH && s == 0) dft8_zh<SIGN>(v);
       else dft8<SIGN>(v);
       if (!last) {
-        Cx<R>* zw = z + sidx<R, LOGM, OP>(p, (b - j) * P + j);
+        const int zw = sidx<R, LOGM, OP>(p, (b - j) * P + j);
 #pragma unroll
-        for (int r = 0; r < P; ++r) zw[padded<R, LOGM>(r * Ls)] = v[r];
+        for (int r = 0; r < P; ++r) xst<R, LOGM, OP>(z, zw + padded<R, LOGM>(r * Ls), v[r]);
       }
       Ls *= P;
     } else {
@@ -364,9 +378,9 @@ __device__ __forceinline__ void fast_stages(Cx<R> (&v)[P], Cx<R>* z, int p, int 
     }
     if (!last) {
       line_sync<R, LOGM, OP, P>(lanes_across_lines, p);
-      const Cx<R>* zr = z + sidx<R, LOGM, OP>(p, b);
+      const int zr = sidx<R, LOGM, OP>(p, b);
 #pragma unroll
-      for (int r = 0; r < P; ++r) v[r] = zr[padded<R, LOGM>(r * T)];
+      for (int r = 0; r < P; ++r) v[r] = xld<R, LOGM, OP>(z, zr + padded<R, LOGM>(r * T));
       line_sync<R, LOGM, OP, P>(lanes_across_lines, p);
     }
   }
@@ -432,6 +446,8 @@ template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
   return sizeof(R) == 4 && fast_pts<R>(logm) == 16
              ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)  // 16 points: 64 registers a thread
+         : sizeof(R) == 4 && op == OP_CSUM
+             ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)  // the sum's terms: ~0.5 KB of spill at 32 registers
          : sizeof(R) == 4
              ? (op == OP_C2R && fast_threads<R>(logm, op) >= 1024
                     ? 1  // c2r at 1024 threads spills heavily at 32 registers
@@ -573,13 +589,39 @@ __device__ __forceinline__ Cx<R> x00_out(Cx<R> z, int odd) {
   return odd ? mul_i(z) : z;
 }
 
-// One tile of a pass: load (from `src`: the pass input in global memory, or
-// a copy of the tile's input lines in shared memory), stages, store.  `src`
-// is addressed as src[soff + pos * ssa + line * sst] (soff < 0: the tile's
-// offset in the pass input).
+// State of one tile of the register pass between its load and its store.
+struct FastTile {
+  TileOrigin o;
+  int64_t t0, ooff, didx, ioff;
+  int nvalid, ncl_valid;  // lines (complex lines) of the tile with data
+  int emax, emax_out;     // dd: exponent of the loaded values, of the outputs
+};
+
+// Tile `bid` of the pass (valid == false: a tile without lines, whose loads
+// and stores are all masked)
+template <typename R, int LOGM, int OP>
+__device__ __forceinline__ FastTile fast_tile_begin(const FastArgs& a, int64_t bid, int64_t soff, bool valid) {
+  constexpr bool packed = fast_packed(OP);
+  constexpr int TW = fast_tw<R>(LOGM, OP);
+  const int lines = packed ? 2 * TW : TW;
+  FastTile s;
+  s.o = tile_origin(a, (unsigned)bid, lines);
+  s.t0 = s.o.t0;
+  s.ooff = s.o.ooff;
+  s.didx = s.o.didx;
+  s.ioff = soff >= 0 ? soff : s.o.ioff;
+  s.nvalid = valid ? (int)min((int64_t)lines, a.nt - s.t0) : 0;
+  s.ncl_valid = packed ? (s.nvalid + 1) / 2 : s.nvalid;
+  s.emax = s.emax_out = 0;
+  return s;
+}
+
+// Load of a tile: v[r] = line p, element b + r T (the stage-1 Stockham
+// inputs), converted to the arithmetic type; dd: the tile's exponents in s.
 template <typename R, int LOGM, int SIGN, int OP, int IOM>
-__device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
-                                              int64_t soff, int64_t ssa, int64_t sst) {
+__device__ __forceinline__ void fast_tile_load(const FastArgs& a, int64_t bid, const void* src, int64_t ssa,
+                                               int64_t sst, int p, int b, FastTile& s,
+                                               Cx<R> (&v)[fast_pts<R>(LOGM)]) {
   using IO = FastIO<R>;
   constexpr bool IN_DD = IO::kDD && (IOM & 1) != 0;   // input in dd form
   constexpr bool OUT_DD = IO::kDD && (IOM & 2) != 0;  // output in dd form
@@ -589,23 +631,11 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   constexpr int P = fast_pts<R>(LOGM);  // points a thread
   constexpr int T = M / P;
   constexpr int TW = fast_tw<R>(LOGM, OP);
-
-  const int tid = threadIdx.x;
-  int p, b;
-  if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
-
-  constexpr bool packed = fast_packed(OP);
-  const int lines = packed ? 2 * TW : TW;
-  const TileOrigin o = tile_origin(a, (unsigned)bid, lines);
-  const int64_t t0 = o.t0, ooff = o.ooff, didx = o.didx;
-  int64_t ioff = o.ioff;
-  const int nvalid = (int)min((int64_t)lines, a.nt - t0);
-  const int ncl_valid = packed ? (nvalid + 1) / 2 : nvalid;  // complex lines with data
-  if (soff >= 0) ioff = soff;
-
-  // ---- load: v[r] = line p, element b + r T (stage-1 Stockham inputs) ----
-  Cx<R> v[P];
-  int emax = 0, emax_out = 0;
+  const TileOrigin& o = s.o;
+  const int64_t t0 = s.t0, didx = s.didx, ioff = s.ioff;
+  const int nvalid = s.nvalid, ncl_valid = s.ncl_valid;
+  int& emax = s.emax;
+  int& emax_out = s.emax_out;
   if constexpr (IO::kDD) {
     if (!a.self_scale) {
       emax = *a.emax_ptr;
@@ -834,14 +864,27 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       v[r] = mk(A.re - B.im, A.im + B.re);
     }
   }
+}
 
-  // per-line exponents of a self-scaled pass, for the stores of other lines
-  __shared__ int lexp[TW];
-  if (IO::kDD && a.self_scale && b == 0) lexp[p] = emax;
-
-  // ---- stages ----
-  fast_stages<R, LOGM, SIGN, OP, P>(v, z, p, b, a.tw, a.lmap_tile != 0);
-
+// Store of a tile from the stage outputs v (directly, or through z in
+// shared memory for the transposed layouts and the r2c split); lexp: the
+// per-line exponents of a self-scaled dd pass.
+template <typename R, int LOGM, int SIGN, int OP, int IOM>
+__device__ __forceinline__ void fast_tile_store(const FastArgs& a, int64_t bid, int p, int b, const FastTile& s,
+                                                Cx<R> (&v)[fast_pts<R>(LOGM)], Cx<R>* z, const int* lexp) {
+  using IO = FastIO<R>;
+  constexpr bool IN_DD = IO::kDD && (IOM & 1) != 0;   // input in dd form
+  constexpr bool OUT_DD = IO::kDD && (IOM & 2) != 0;  // output in dd form
+  using MR = typename IO::MR;
+  using MC = typename IO::MC;
+  constexpr int M = 1 << LOGM;
+  constexpr int P = fast_pts<R>(LOGM);  // points a thread
+  constexpr int T = M / P;
+  constexpr int TW = fast_tw<R>(LOGM, OP);
+  const int tid = threadIdx.x;
+  const int64_t t0 = s.t0, ooff = s.ooff, didx = s.didx;
+  const int nvalid = s.nvalid;
+  const int emax_out = s.emax_out;
   // ---- store ----
   if (a.deriv == 2 && a.store_direct && OP == OP_C2C) {
 #pragma unroll
@@ -1048,6 +1091,31 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
       if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
     }
   }
+}
+
+// One tile of the register pass for float and dd (fx: fast_tile_fx): load
+// (from `src`: the pass input in global memory, or a copy of the tile's input
+// lines in shared memory), stages, store.  `src` is addressed as
+// src[soff + pos * ssa + line * sst] (soff < 0: the tile's offset in the pass
+// input).
+template <typename R, int LOGM, int SIGN, int OP, int IOM>
+__device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx<R>* z, const void* src,
+                                              int64_t soff, int64_t ssa, int64_t sst) {
+  using IO = FastIO<R>;
+  constexpr int P = fast_pts<R>(LOGM);
+  constexpr int T = (1 << LOGM) / P;
+  constexpr int TW = fast_tw<R>(LOGM, OP);
+  const int tid = threadIdx.x;
+  int p, b;
+  if (a.lmap_tile) { p = tid % TW; b = tid / TW; } else { b = tid % T; p = tid / T; }
+  FastTile s = fast_tile_begin<R, LOGM, OP>(a, bid, soff, true);
+  Cx<R> v[P];
+  fast_tile_load<R, LOGM, SIGN, OP, IOM>(a, bid, src, ssa, sst, p, b, s, v);
+  // per-line exponents of a self-scaled pass, for the stores of other lines
+  __shared__ int lexp[TW];
+  if (IO::kDD && a.self_scale && b == 0) lexp[p] = s.emax;
+  fast_stages<R, LOGM, SIGN, OP, P>(v, z, p, b, a.tw, a.lmap_tile != 0);
+  fast_tile_store<R, LOGM, SIGN, OP, IOM>(a, bid, p, b, s, v, z, lexp);
 }
 
 // One tile of an fx pass (R = fx).  Load: each complex line gets the scale

@@ -1064,6 +1064,11 @@ int launch_pass(int real_bytes, const PassArgs& A, int64_t grid, int threads, si
 int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+
+// The register pass kernel of a plain (not TMA-fed, not tensor-core) launch.
+static int launch_plain(const pfgb_plan* P, const Pass& ps, const FastArgs& F, int64_t grid, cudaStream_t s) {
+  return P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, s) : launch_fast_f32(ps.logm, ps.sign, F, grid, s);
+}
 int launch_fast_fx(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_tma_f32(int logm, int sign, const FastArgs& A, cudaStream_t s);
 int launch_tc(int logm, int sign, const FastArgs& A, cudaStream_t s);
@@ -1530,8 +1535,7 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
         rc = P->rb == 8 ? launch_fast_tma_dd(ps.logm, ps.sign, F, s)
                         : launch_fast_tma_f32(ps.logm, ps.sign, F, s);
       } else {
-        rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, s)
-                        : launch_fast_f32(ps.logm, ps.sign, F, grid, s);
+        rc = launch_plain(P, ps, F, grid, s);
       }
       if (rc) return rc;
     } else if (ps.mr) {
@@ -2458,7 +2462,7 @@ static int autotune_passes(pfgb_plan* P) {
         for (int it = 0; it < 7 && !rc; ++it) {
           cudaEventRecord(ea, 0);
           if (v == 0) {
-            rc = P->rb == 8 ? launch_fast_dd(ps.logm, ps.sign, F, grid, 0) : launch_fast_f32(ps.logm, ps.sign, F, grid, 0);
+            rc = launch_plain(P, ps, F, grid, 0);
           } else {
             F.total = grid;
             F.err = P->emax_dev + 1;
