@@ -43,6 +43,19 @@ enum PassOp : int {
   // (lines longer than one pass takes): c2c along n2 whose outputs are
   // multiplied by W_M^(n1 k2), n1 the index along the line's other part
   OP_C2CT = 8,
+  // register Stockham pass only: REDFT10 / RODFT10 (D2) and REDFT01 / RODFT01
+  // (D3) of a power-of-two length n through one n-point complex DFT, on
+  // complex lines (D2C, D3C) or on two real lines packed in one complex line
+  // (D2R, D3R).  D2: the DFT of v[m] = x[2m], v[n-1-m] = x[2m+1] (m < n/2),
+  // then Y[k] = w_k V[k] + conj(w_k) V[n-k], w_k = exp(-i pi k / (2n)).  D3:
+  // the inverse DFT of conj(w_k) (y[k] - i y[n-k]) (y[n] = 0), then
+  // out[2m] = v[m], out[2m+1] = v[n-1-m].  The odd kinds (RODFT10 / RODFT01)
+  // alternate the sign of the even kind's input (D2) or output (D3) and
+  // reverse its output (D2) or input (D3).
+  OP_D2C = 9,
+  OP_D2R = 10,
+  OP_D3C = 11,
+  OP_D3R = 12,
 };
 
 // FFTW r2r kind codes.

@@ -43,8 +43,9 @@ struct FastArgs {
   // the dimension of role t4_role (1 tile, 2 + o outer)
   const void* t4_tab;
   int t4_role;
-  int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R
-  int r2r_odd;     // OP_X00C / OP_X00R: 0 REDFT00 (even extension), 1 RODFT00 (odd)
+  int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R, OP_D2C ...
+  int r2r_odd;     // OP_X00C / R, OP_D2C / R, OP_D3C / R: 0 the REDFT kind, 1 the RODFT kind
+  const void* d23_tab;  // OP_D2* / OP_D3*: w_k = exp(-i pi k / (2n)), k < n, as Cx<R>
   int n_in, n_out;
   int lmap_tile;     // lanes along the tile dimension (tile dim contiguous in input)
   int store_direct;  // store from registers with the load mapping
@@ -171,7 +172,11 @@ __host__ __device__ constexpr int fast_pts(int logm) {
 
 // Operations of the fast pass that pack two real lines in one complex line.
 __host__ __device__ constexpr bool fast_packed(int op) {
-  return op == OP_R2C || op == OP_C2R || op == OP_X00R;
+  return op == OP_R2C || op == OP_C2R || op == OP_X00R || op == OP_D2R || op == OP_D3R;
+}
+// REDFT10 / 01 and RODFT10 / 01 through one DFT of their length
+__host__ __device__ constexpr bool fast_d23(int op) {
+  return op == OP_D2C || op == OP_D2R || op == OP_D3C || op == OP_D3R;
 }
 
 template <typename R>
@@ -446,8 +451,9 @@ template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
   return sizeof(R) == 4 && fast_pts<R>(logm) == 16
              ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)  // 16 points: 64 registers a thread
-         : sizeof(R) == 4 && op == OP_CSUM
-             ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)  // the sum's terms: ~0.5 KB of spill at 32 registers
+         : sizeof(R) == 4 && (op == OP_CSUM || fast_d23(op))
+             // the sum's terms; the two loads a position of D3: ~0.2-0.5 KB of spill at 32 registers
+             ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)
          : sizeof(R) == 4
              ? (op == OP_C2R && fast_threads<R>(logm, op) >= 1024
                     ? 1  // c2r at 1024 threads spills heavily at 32 registers
@@ -456,6 +462,7 @@ __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
                            ? (op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS)
                            : 2048 / fast_threads<R>(logm, op)))
          : fast_threads<R>(logm, op) >= 512 ? 1
+         : fast_d23(op) ? 3  // two loads a position (D3) or two real lines (D2R / D3R): ~0.2-0.5 KB of spill at 64 registers
          : PFGB_FAST_DD_MINBLOCKS <= 0 ? 512 / fast_threads<R>(logm, op)
          : (op == OP_C2R && !(iom & 1) && PFGB_FAST_DD_MINBLOCKS > 4) ? 4
                                                                      : PFGB_FAST_DD_MINBLOCKS;
@@ -791,6 +798,100 @@ __device__ __forceinline__ void fast_tile_load(const FastArgs& a, int64_t bid, c
       const Cx<R> y = mk(mkr<R>(ra[r], emax), mkr<R>(rb[r], emax));
       v[r] = sgs[r] < 0 ? -y : y;
     }
+  } else if constexpr (fast_d23(OP)) {
+    // REDFT10 / RODFT10 (D2) and REDFT01 / RODFT01 (D3) through one M-point
+    // DFT (the identities at OP_D2C in pfgb_device.cuh), on complex lines or
+    // two real lines packed in one.  Register r holds the DFT input at
+    // position pos = b + r T: D2 the source x[ja] (negated at odd ja for
+    // RODFT10), D3 conj(w_pos) (y[ja] - i y[jb]) (jb < 0: y[M] = 0).
+    constexpr bool D3 = OP == OP_D3C || OP == OP_D3R;
+    constexpr bool PK = OP == OP_D2R || OP == OP_D3R;
+    const int odd = a.r2r_odd;
+    int ja[P], jb[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      const int pos = b + r * T;
+      if constexpr (!D3) {
+        ja[r] = pos < M / 2 ? 2 * pos : 2 * (M - 1 - pos) + 1;
+        jb[r] = -1;
+      } else {
+        ja[r] = odd ? M - 1 - pos : pos;
+        jb[r] = pos == 0 ? -1 : (odd ? pos - 1 : M - pos);
+      }
+    }
+    Cx<R> ya[P], yb[P];
+    if constexpr (PK) {
+      const MR* in = reinterpret_cast<const MR*>(src) + ioff;
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      MR a0[P], a1[P], b0[P], b1[P];
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        const int64_t oa = (int64_t)ja[r] * ssa, ob = (int64_t)(jb[r] < 0 ? 0 : jb[r]) * ssa;
+        a0[r] = i0 < nvalid ? in[oa + (int64_t)i0 * sst] : MR(0);
+        a1[r] = i1 < nvalid ? in[oa + (int64_t)i1 * sst] : MR(0);
+        b0[r] = (D3 && jb[r] >= 0 && i0 < nvalid) ? in[ob + (int64_t)i0 * sst] : MR(0);
+        b1[r] = (D3 && jb[r] >= 0 && i1 < nvalid) ? in[ob + (int64_t)i1 * sst] : MR(0);
+      }
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < P; ++r)
+            emx = max(emx, max(max(dexp_u(a0[r]), dexp_u(a1[r])), max(dexp_u(b0[r]), dexp_u(b1[r]))));
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax_out = emax + a.emax_shift;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        ya[r] = mk(mkr<R>(a0[r], emax), mkr<R>(a1[r], emax));
+        yb[r] = mk(mkr<R>(b0[r], emax), mkr<R>(b1[r], emax));
+      }
+    } else if (IO::kDD && IN_DD) {
+      const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        ya[r] = ld_dd4<R>(p < nvalid ? in[(int64_t)ja[r] * ssa] : z4);
+        yb[r] = ld_dd4<R>((D3 && jb[r] >= 0 && p < nvalid) ? in[(int64_t)jb[r] * ssa] : z4);
+        if (IO::kDD && a.te_rescale && p < nvalid) {
+          ya[r] = scale_pow2(ya[r], te_factor(a, o.tebase, t0 + p, ja[r], emax));
+          if (D3 && jb[r] >= 0) yb[r] = scale_pow2(yb[r], te_factor(a, o.tebase, t0 + p, jb[r], emax));
+        }
+      }
+    } else {
+      const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
+      MC ra[P], rb[P];
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        ra[r] = p < nvalid ? in[(int64_t)ja[r] * ssa] : MC{0, 0};
+        rb[r] = (D3 && jb[r] >= 0 && p < nvalid) ? in[(int64_t)jb[r] * ssa] : MC{0, 0};
+      }
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < P; ++r)
+            emx = max(emx, max(max(dexp_u(ra[r].x), dexp_u(ra[r].y)), max(dexp_u(rb[r].x), dexp_u(rb[r].y))));
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax_out = emax + a.emax_shift;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        ya[r] = mk(mkr<R>(ra[r].x, emax), mkr<R>(ra[r].y, emax));
+        yb[r] = mk(mkr<R>(rb[r].x, emax), mkr<R>(rb[r].y, emax));
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      if constexpr (!D3) {
+        v[r] = (odd && (ja[r] & 1)) ? -ya[r] : ya[r];
+      } else {
+        const Cx<R> u = mk(ya[r].re + yb[r].im, ya[r].im - yb[r].re);  // y[ja] - i y[jb]
+        v[r] = u * conj(ldg_tw<R>(a.d23_tab, b + r * T));
+      }
+    }
   } else if constexpr (OP == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
@@ -899,7 +1000,7 @@ __device__ __forceinline__ void fast_tile_store(const FastArgs& a, int64_t bid, 
 #pragma unroll
     for (int r = 0; r < P; ++r) v[r] = tw_mul<R, SIGN>(v[r], a.t4_tab, (int)(n1 * (int64_t)(b + r * T)));
   }
-  if (a.store_direct && OP != OP_R2C) {
+  if (a.store_direct && OP != OP_R2C && !fast_d23(OP)) {
     if constexpr (OP == OP_C2C || OP == OP_CSUM || OP == OP_C2CT) {
       if (p < nvalid) {
         if (IO::kDD && OUT_DD) {
@@ -1076,6 +1177,47 @@ __device__ __forceinline__ void fast_tile_store(const FastArgs& a, int64_t bid, 
       const int eo = line_emax_out(q);
       if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, eo);
       if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
+    }
+  } else if constexpr (fast_d23(OP)) {
+    // D2: Y[kk] = w_kk V[kk] + conj(w_kk) V[M - kk] at output k = kk (REDFT10)
+    // or M - 1 - kk (RODFT10); D3: out[k] = v[k / 2] (k even) or
+    // v[M - 1 - (k - 1) / 2] (k odd), negated at odd k for RODFT01
+    constexpr bool D3 = OP == OP_D3C || OP == OP_D3R;
+    constexpr bool PK = OP == OP_D2R || OP == OP_D3R;
+    const int odd = a.r2r_odd;
+    const int tot = TW * M;
+    for (int e = tid; e < tot; e += nth) {
+      int q, k;
+      if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % M; q = e / M; }
+      if (!PK && q >= nvalid) continue;
+      Cx<R> y;
+      if constexpr (!D3) {
+        const int kk = odd ? M - 1 - k : k;
+        const Cx<R> f = z[sidx<R, LOGM, OP>(q, kk)];
+        const Cx<R> g = z[sidx<R, LOGM, OP>(q, (M - kk) & (M - 1))];
+        const Cx<R> w = ldg_tw<R>(a.d23_tab, kk);
+        y = f * w + g * conj(w);
+      } else {
+        y = z[sidx<R, LOGM, OP>(q, (k & 1) ? M - 1 - (k >> 1) : (k >> 1))];
+        if (odd && (k & 1)) y = -y;
+      }
+      y = apply_scale(y, a);
+      const int64_t off = (int64_t)k * a.out_sa;
+      if constexpr (PK) {
+        MR* out = reinterpret_cast<MR*>(a.out) + ooff;
+        const int i0 = 2 * q, i1 = 2 * q + 1;
+        const int eo = line_emax_out(q);
+        if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, eo);
+        if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
+      } else if (IO::kDD && OUT_DD) {
+        reinterpret_cast<float4*>(a.out)[ooff + off + (int64_t)q * a.out_st] = st_dd4(y);
+      } else {
+        const int eo = line_emax_out(q);
+        MC o;
+        o.x = outr<R>(y.re, eo);
+        o.y = outr<R>(y.im, eo);
+        reinterpret_cast<MC*>(a.out)[ooff + off + (int64_t)q * a.out_st] = o;
+      }
     }
   } else {  // C2R with a transposed output layout
     MR* out = reinterpret_cast<MR*>(a.out) + ooff;

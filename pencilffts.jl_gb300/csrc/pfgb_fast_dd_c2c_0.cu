@@ -18,6 +18,16 @@ int launch_fast_dd_x00r_0(int logm, int sign, const FastArgs& A, int64_t grid, c
 int launch_fast_dd_csum_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_csum_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_c2ct_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d3c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d2c_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d3c_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d2c_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d3c_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d2c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d3c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d2r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d3r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
 int launch_fast_dd_c2c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   return launch_fast_op<dd, OP_C2C, 0>(logm, sign, A, grid, s);
@@ -44,6 +54,16 @@ int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStre
     case OP_CSUM * 4 + 0: return launch_fast_dd_csum_0(logm, sign, A, grid, s);
     case OP_CSUM * 4 + 2: return launch_fast_dd_csum_2(logm, sign, A, grid, s);
     case OP_C2CT * 4 + 0: return launch_fast_dd_c2ct_0(logm, sign, A, grid, s);
+    case OP_D2C * 4 + 0: return launch_fast_dd_d2c_0(logm, sign, A, grid, s);
+    case OP_D3C * 4 + 0: return launch_fast_dd_d3c_0(logm, sign, A, grid, s);
+    case OP_D2C * 4 + 1: return launch_fast_dd_d2c_1(logm, sign, A, grid, s);
+    case OP_D3C * 4 + 1: return launch_fast_dd_d3c_1(logm, sign, A, grid, s);
+    case OP_D2C * 4 + 2: return launch_fast_dd_d2c_2(logm, sign, A, grid, s);
+    case OP_D3C * 4 + 2: return launch_fast_dd_d3c_2(logm, sign, A, grid, s);
+    case OP_D2C * 4 + 3: return launch_fast_dd_d2c_3(logm, sign, A, grid, s);
+    case OP_D3C * 4 + 3: return launch_fast_dd_d3c_3(logm, sign, A, grid, s);
+    case OP_D2R * 4 + 0: return launch_fast_dd_d2r_0(logm, sign, A, grid, s);
+    case OP_D3R * 4 + 0: return launch_fast_dd_d3r_0(logm, sign, A, grid, s);
     default: return PFGB_ERR_UNSUPPORTED;
   }
 }

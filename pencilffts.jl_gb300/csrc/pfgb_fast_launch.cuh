@@ -57,6 +57,12 @@ template <typename R, int OP, int IOM>
 static int launch_fast_op_fwd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   return sign < 0 ? launch_fast_sign<R, -1, OP, IOM>(logm, A, grid, s) : PFGB_ERR_UNSUPPORTED;
 }
+// Operations whose DFT runs with the backward sign only (REDFT01 / RODFT01
+// through an inverse DFT)
+template <typename R, int OP, int IOM>
+static int launch_fast_op_bwd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return sign > 0 ? launch_fast_sign<R, 1, OP, IOM>(logm, A, grid, s) : PFGB_ERR_UNSUPPORTED;
+}
 
 // TMA-fed persistent form (c2r passes); A.total == 0 only configures it.
 template <typename R, int LOGM, int SIGN, int IOM>

@@ -132,6 +132,8 @@ struct Pass {
   int t4_dim = -1;
   int64_t t4_M = 0;
   const void* t4_tab = nullptr;
+  // REDFT10 / 01, RODFT10 / 01 on the register pass: w_k = exp(-i pi k / (2n))
+  const void* d23_tab = nullptr;
   bool bs = false;
   int logl = 0;
   const void* bs_chirp = nullptr;
@@ -664,6 +666,33 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   // on the generic kernel)
   const bool x00 = (ps.op == OP_R2R_C || ps.op == OP_R2R_R) &&
                    (ps.r2r_kind == K_REDFT00 || ps.r2r_kind == K_RODFT00) && !P->fx;
+  // REDFT10 / RODFT10 and REDFT01 / RODFT01 of a power-of-two length n
+  // (8 <= n <= 4096) take the register pass through one n-point DFT
+  {
+    const int n = (int)n_in;
+    const bool d2 = ps.r2r_kind == K_REDFT10 || ps.r2r_kind == K_RODFT10;
+    const bool d3 = ps.r2r_kind == K_REDFT01 || ps.r2r_kind == K_RODFT01;
+    if ((ps.op == OP_R2R_C || ps.op == OP_R2R_R) && (d2 || d3) && !P->fx && n >= 8 && n <= 4096 &&
+        (n & (n - 1)) == 0 && !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+      ps.fast = true;
+      const bool cplx = ps.op == OP_R2R_C;
+      ps.fop = d2 ? (cplx ? OP_D2C : OP_D2R) : (cplx ? OP_D3C : OP_D3R);
+      ps.sign = d2 ? -1 : 1;
+      ps.logm = 0;
+      while ((1 << ps.logm) < n) ++ps.logm;
+      std::vector<std::complex<ld>> w(n);
+      for (int k = 0; k < n; ++k) w[k] = expi_pi(k, 2 * (int64_t)n);  // exp(-i pi k / (2n))
+      int rc2 = upload_fast_table(P, n, &ps.ftw);
+      if (!rc2) rc2 = upload_fast_vec(P, "d23/" + std::to_string(n), w, &ps.d23_tab);
+      if (rc2) return rc2;
+      const bool packed = fast_packed(ps.fop);
+      ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.fop) : fast_tw<float>(ps.logm, ps.fop);
+      ps.lines = packed ? 2 * ps.clines : ps.clines;
+      ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm, ps.fop) : fast_threads<float>(ps.logm, ps.fop);
+      ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm, ps.fop) : fast_smem<float>(ps.logm, ps.fop);
+      return PFGB_OK;
+    }
+  }
   if ((ps.op == OP_C2C || ps.op == OP_R2C || ps.op == OP_C2R || x00) && ps.L == 0 && M >= 8 &&
       M <= 4096 && (M & (M - 1)) == 0 &&
       !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
@@ -953,7 +982,8 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.t4_tab = ps.t4_tab;
   F.t4_role = ps.t4_dim >= 0 ? pass_role(ps, ps.t4_dim) : 0;
   F.op = ps.fop;
-  F.r2r_odd = ps.r2r_kind == K_RODFT00 ? 1 : 0;
+  F.r2r_odd = (ps.r2r_kind == K_RODFT00 || ps.r2r_kind == K_RODFT10 || ps.r2r_kind == K_RODFT01) ? 1 : 0;
+  F.d23_tab = ps.d23_tab;
   F.n_in = A.n_in;
   F.n_out = A.n_out;
   F.lmap_tile = A.in_tfast;
@@ -2282,7 +2312,9 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
       auto& v = dir->passes;
       // passes that exchange dd-form data with their neighbours (packed real
       // R2R lines always read and write doubles)
-      auto chains = [](const Pass& q) { return q.fast && q.fop != OP_X00R && !q.four; };
+      auto chains = [](const Pass& q) {
+        return q.fast && q.fop != OP_X00R && q.fop != OP_D2R && q.fop != OP_D3R && !q.four;
+      };
       for (size_t i = 0; i < v.size(); ++i) {
         if (!v[i].fast) continue;
         const bool prev = chains(v[i]) && i > 0 && chains(v[i - 1]);

@@ -23,10 +23,11 @@ INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["pfgb_persist.cu", "pfgb_plan.cu", "pfgb_kernels.cu", "pfgb_noalloc.cu", "pfgb_tc.cu"] + [
-    f"pfgb_fast_f32_{op}.cu" for op in ("c2c", "r2c", "c2r", "x00")] + [
+    f"pfgb_fast_f32_{op}.cu" for op in ("c2c", "r2c", "c2r", "x00", "d23")] + [
     f"pfgb_fast_{t}_{op}_{iom}.cu" for t in ("dd", "fx")
     for op, ioms in (("c2c", (0, 1, 2, 3)), ("r2c", (0, 2)), ("c2r", (0, 1))) for iom in ioms] + [
     f"pfgb_fast_dd_x00c_{iom}.cu" for iom in (0, 1, 2, 3)] + ["pfgb_fast_dd_x00r_0.cu"] + [
+    f"pfgb_fast_dd_d23c_{iom}.cu" for iom in (0, 1, 2, 3)] + ["pfgb_fast_dd_d23r_0.cu"] + [
     f"pfgb_fast_dd_csum_{iom}.cu" for iom in (0, 2)] + ["pfgb_fast_dd_c2ct_0.cu"] + [
     f"pfgb_mr_{t}_{op}_{r0}.cu" for t in ("f32", "dd") for op in ("c2c", "r2c", "c2r") for r0 in (3, 5)] + [
     f"pfgb_bs_{t}_{op}.cu" for t in ("f32", "dd") for op in ("c2c", "r2c", "c2r")]
