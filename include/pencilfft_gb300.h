@@ -88,9 +88,11 @@ typedef struct pfgb_plan_desc {
  *             double-float (two FP32 values, 48-bit significand, on the FP32
  *             pipes) the c2c / r2c / c2r lines of up to 4096 points (power of
  *             two), 3 * 2^k and 5 * 2^k points, and any other length up to
- *             2048 (Bluestein), and REDFT00 / RODFT00 lines of 2^k +- 1
- *             points; the remaining lines (other R2R kinds and lengths,
- *             longer lines) in native FP64.  Both meet a relative L2 error of
+ *             2048 (Bluestein), REDFT00 / RODFT00 lines of 2^k +- 1 points
+ *             and REDFT10 / REDFT01 / RODFT10 / RODFT01 / DHT lines of 2^k
+ *             points;
+ *             the remaining lines (other R2R kinds and lengths, longer lines)
+ *             in native FP64.  Both meet a relative L2 error of
  *             1e-13.
  *   NATIVE:   Float64 plans compute every line in native FP64 (GB300's FP64
  *             rate is about 1/70 of its FP32 rate).

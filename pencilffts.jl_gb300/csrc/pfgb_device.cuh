@@ -51,7 +51,9 @@ enum PassOp : int {
   // the inverse DFT of conj(w_k) (y[k] - i y[n-k]) (y[n] = 0), then
   // out[2m] = v[m], out[2m+1] = v[n-1-m].  The odd kinds (RODFT10 / RODFT01)
   // alternate the sign of the even kind's input (D2) or output (D3) and
-  // reverse its output (D2) or input (D3).
+  // reverse its output (D2) or input (D3).  The DHT is D2 without the
+  // reordering and with w_k = (1 + i) / 2 (H[k] = Re F[k] - Im F[k] for real
+  // lines, by linearity for complex ones).
   OP_D2C = 9,
   OP_D2R = 10,
   OP_D3C = 11,

@@ -44,7 +44,7 @@ struct FastArgs {
   const void* t4_tab;
   int t4_role;
   int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R, OP_D2C ...
-  int r2r_odd;     // OP_X00C / R, OP_D2C / R, OP_D3C / R: 0 the REDFT kind, 1 the RODFT kind
+  int r2r_odd;     // OP_X00C / R, OP_D2C / R, OP_D3C / R: 0 the REDFT kind, 1 the RODFT kind, 2 DHT (D2)
   const void* d23_tab;  // OP_D2* / OP_D3*: w_k = exp(-i pi k / (2n)), k < n, as Cx<R>
   int n_in, n_out;
   int lmap_tile;     // lanes along the tile dimension (tile dim contiguous in input)
@@ -799,11 +799,12 @@ __device__ __forceinline__ void fast_tile_load(const FastArgs& a, int64_t bid, c
       v[r] = sgs[r] < 0 ? -y : y;
     }
   } else if constexpr (fast_d23(OP)) {
-    // REDFT10 / RODFT10 (D2) and REDFT01 / RODFT01 (D3) through one M-point
-    // DFT (the identities at OP_D2C in pfgb_device.cuh), on complex lines or
-    // two real lines packed in one.  Register r holds the DFT input at
-    // position pos = b + r T: D2 the source x[ja] (negated at odd ja for
-    // RODFT10), D3 conj(w_pos) (y[ja] - i y[jb]) (jb < 0: y[M] = 0).
+    // REDFT10 / RODFT10 / DHT (D2) and REDFT01 / RODFT01 (D3) through one
+    // M-point DFT (the identities at OP_D2C in pfgb_device.cuh), on complex
+    // lines or two real lines packed in one.  Register r holds the DFT input
+    // at position pos = b + r T: D2 the source x[ja] (negated at odd ja for
+    // RODFT10; ja = pos for the DHT), D3 conj(w_pos) (y[ja] - i y[jb])
+    // (jb < 0: y[M] = 0).
     constexpr bool D3 = OP == OP_D3C || OP == OP_D3R;
     constexpr bool PK = OP == OP_D2R || OP == OP_D3R;
     const int odd = a.r2r_odd;
@@ -812,7 +813,7 @@ __device__ __forceinline__ void fast_tile_load(const FastArgs& a, int64_t bid, c
     for (int r = 0; r < P; ++r) {
       const int pos = b + r * T;
       if constexpr (!D3) {
-        ja[r] = pos < M / 2 ? 2 * pos : 2 * (M - 1 - pos) + 1;
+        ja[r] = odd == 2 ? pos : pos < M / 2 ? 2 * pos : 2 * (M - 1 - pos) + 1;  // DHT: in order
         jb[r] = -1;
       } else {
         ja[r] = odd ? M - 1 - pos : pos;
@@ -886,7 +887,7 @@ __device__ __forceinline__ void fast_tile_load(const FastArgs& a, int64_t bid, c
 #pragma unroll
     for (int r = 0; r < P; ++r) {
       if constexpr (!D3) {
-        v[r] = (odd && (ja[r] & 1)) ? -ya[r] : ya[r];
+        v[r] = (odd == 1 && (ja[r] & 1)) ? -ya[r] : ya[r];
       } else {
         const Cx<R> u = mk(ya[r].re + yb[r].im, ya[r].im - yb[r].re);  // y[ja] - i y[jb]
         v[r] = u * conj(ldg_tw<R>(a.d23_tab, b + r * T));
@@ -1192,7 +1193,7 @@ __device__ __forceinline__ void fast_tile_store(const FastArgs& a, int64_t bid, 
       if (!PK && q >= nvalid) continue;
       Cx<R> y;
       if constexpr (!D3) {
-        const int kk = odd ? M - 1 - k : k;
+        const int kk = odd == 1 ? M - 1 - k : k;
         const Cx<R> f = z[sidx<R, LOGM, OP>(q, kk)];
         const Cx<R> g = z[sidx<R, LOGM, OP>(q, (M - kk) & (M - 1))];
         const Cx<R> w = ldg_tw<R>(a.d23_tab, kk);

@@ -666,11 +666,12 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   // on the generic kernel)
   const bool x00 = (ps.op == OP_R2R_C || ps.op == OP_R2R_R) &&
                    (ps.r2r_kind == K_REDFT00 || ps.r2r_kind == K_RODFT00) && !P->fx;
-  // REDFT10 / RODFT10 and REDFT01 / RODFT01 of a power-of-two length n
+  // REDFT10 / RODFT10, REDFT01 / RODFT01 and DHT of a power-of-two length n
   // (8 <= n <= 4096) take the register pass through one n-point DFT
   {
     const int n = (int)n_in;
-    const bool d2 = ps.r2r_kind == K_REDFT10 || ps.r2r_kind == K_RODFT10;
+    const bool dht = ps.r2r_kind == K_DHT;
+    const bool d2 = ps.r2r_kind == K_REDFT10 || ps.r2r_kind == K_RODFT10 || dht;
     const bool d3 = ps.r2r_kind == K_REDFT01 || ps.r2r_kind == K_RODFT01;
     if ((ps.op == OP_R2R_C || ps.op == OP_R2R_R) && (d2 || d3) && !P->fx && n >= 8 && n <= 4096 &&
         (n & (n - 1)) == 0 && !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
@@ -681,9 +682,10 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
       ps.logm = 0;
       while ((1 << ps.logm) < n) ++ps.logm;
       std::vector<std::complex<ld>> w(n);
-      for (int k = 0; k < n; ++k) w[k] = expi_pi(k, 2 * (int64_t)n);  // exp(-i pi k / (2n))
+      for (int k = 0; k < n; ++k)  // exp(-i pi k / (2n)); DHT: (1 + i) / 2
+        w[k] = dht ? std::complex<ld>(0.5L, 0.5L) : expi_pi(k, 2 * (int64_t)n);
       int rc2 = upload_fast_table(P, n, &ps.ftw);
-      if (!rc2) rc2 = upload_fast_vec(P, "d23/" + std::to_string(n), w, &ps.d23_tab);
+      if (!rc2) rc2 = upload_fast_vec(P, (dht ? "dht/" : "d23/") + std::to_string(n), w, &ps.d23_tab);
       if (rc2) return rc2;
       const bool packed = fast_packed(ps.fop);
       ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.fop) : fast_tw<float>(ps.logm, ps.fop);
@@ -982,7 +984,9 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.t4_tab = ps.t4_tab;
   F.t4_role = ps.t4_dim >= 0 ? pass_role(ps, ps.t4_dim) : 0;
   F.op = ps.fop;
-  F.r2r_odd = (ps.r2r_kind == K_RODFT00 || ps.r2r_kind == K_RODFT10 || ps.r2r_kind == K_RODFT01) ? 1 : 0;
+  F.r2r_odd = (ps.r2r_kind == K_RODFT00 || ps.r2r_kind == K_RODFT10 || ps.r2r_kind == K_RODFT01) ? 1
+              : ps.r2r_kind == K_DHT                                                             ? 2
+                                                                                                 : 0;
   F.d23_tab = ps.d23_tab;
   F.n_in = A.n_in;
   F.n_out = A.n_out;

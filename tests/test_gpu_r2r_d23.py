@@ -1,5 +1,7 @@
-"""REDFT10 / REDFT01 (DCT-II / DCT-III) and RODFT10 / RODFT01 (DST-II /
-DST-III) of power-of-two length on the register Stockham kernel (GPU).
+"""REDFT10 / REDFT01 (DCT-II / DCT-III), RODFT10 / RODFT01 (DST-II /
+DST-III) and the DHT of power-of-two length on the register Stockham kernel
+(GPU).  The DHT is the DCT-II's post-processing with w = (1 + i) / 2 on the
+DFT of the line in order.
 
 A line of n points is one n-point complex DFT: DCT-II of the reordered line
 v[m] = x[2m], v[n-1-m] = x[2m+1] followed by Y[k] = w_k V[k] + conj(w_k)
@@ -21,11 +23,11 @@ from test_gpu_r2r_fast import assert_fast_on
 
 pytestmark = pytest.mark.gpu
 F64, F32 = np.float64, np.float32
-KINDS = [T.REDFT10, T.REDFT01, T.RODFT10, T.RODFT01]
+KINDS = [T.REDFT10, T.REDFT01, T.RODFT10, T.RODFT01, T.DHT]
 
 
 @pytest.mark.parametrize("real", [F64, F32])
-@pytest.mark.parametrize("kind", KINDS, ids=["REDFT10", "REDFT01", "RODFT10", "RODFT01"])
+@pytest.mark.parametrize("kind", KINDS, ids=["REDFT10", "REDFT01", "RODFT10", "RODFT01", "DHT"])
 @pytest.mark.parametrize("n", [8, 16, 64, 512, 4096])
 def test_d23_real_lines(cuda, real, kind, n):
     """1D real lines, an odd number of them (the last packed pair is half
@@ -36,7 +38,7 @@ def test_d23_real_lines(cuda, real, kind, n):
 
 
 @pytest.mark.parametrize("real", [F64, F32])
-@pytest.mark.parametrize("kind", KINDS, ids=["REDFT10", "REDFT01", "RODFT10", "RODFT01"])
+@pytest.mark.parametrize("kind", KINDS, ids=["REDFT10", "REDFT01", "RODFT10", "RODFT01", "DHT"])
 @pytest.mark.parametrize("pos", ["first", "middle", "last"])
 def test_d23_complex_in_runs(cuda, real, kind, pos):
     """R2R on complex data as the first, middle or last pass of a run of
@@ -59,7 +61,7 @@ def test_d23_complex_in_runs(cuda, real, kind, pos):
 def test_d23_mixed_real_3d(cuda, real):
     """Three packed-real passes of different kinds on a 3D grid, with extra
     dimensions, both output orders."""
-    tr = (T.R2R(T.REDFT10), T.R2R(T.RODFT01), T.R2R(T.REDFT01))
+    tr = (T.R2R(T.REDFT10), T.R2R(T.RODFT01), T.R2R(T.DHT))
     for permute in (True, False):
         plan = P.PencilFFTPlan((16, 64, 8), tr, real, permute_dims=permute, extra_dims=(3,))
         check_plan(plan, seed=6)
