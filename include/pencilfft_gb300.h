@@ -89,8 +89,8 @@ typedef struct pfgb_plan_desc {
  *             pipes) the c2c / r2c / c2r lines of up to 4096 points (power of
  *             two), 3 * 2^k and 5 * 2^k points, and any other length up to
  *             2048 (Bluestein), REDFT00 / RODFT00 lines of 2^k +- 1 points
- *             and REDFT10 / REDFT01 / RODFT10 / RODFT01 / DHT lines of 2^k
- *             points;
+ *             and REDFT10 / REDFT01 / RODFT10 / RODFT01 / DHT / REDFT11 /
+ *             RODFT11 lines of 2^k points;
  *             the remaining lines (other R2R kinds and lengths, longer lines)
  *             in native FP64.  Both meet a relative L2 error of
  *             1e-13.

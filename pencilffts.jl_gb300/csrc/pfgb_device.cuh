@@ -58,6 +58,14 @@ enum PassOp : int {
   OP_D2R = 10,
   OP_D3C = 11,
   OP_D3R = 12,
+  // register Stockham pass only: REDFT11 / RODFT11 (D4) of a power-of-two
+  // length n through one 2n-point DFT: V = DFT_2n of x[j] c_j (j < n, zero
+  // above; c_j = exp(-i pi j / (2n))), then with d_k = exp(-i pi (2k+1) / (4n))
+  // REDFT11: Y[k] = d_k V[k] + conj(d_k) V[2n-1-k], RODFT11: i (d_k V[k] -
+  // conj(d_k) V[2n-1-k]), k < n; complex lines (D4C) or two real lines packed
+  // in one (D4R)
+  OP_D4C = 13,
+  OP_D4R = 14,
 };
 
 // FFTW r2r kind codes.

@@ -45,7 +45,9 @@ struct FastArgs {
   int t4_role;
   int op;          // OP_C2C, OP_R2C, OP_C2R, OP_X00C, OP_X00R, OP_D2C ...
   int r2r_odd;     // OP_X00C / R, OP_D2C / R, OP_D3C / R: 0 the REDFT kind, 1 the RODFT kind, 2 DHT (D2)
-  const void* d23_tab;  // OP_D2* / OP_D3*: w_k = exp(-i pi k / (2n)), k < n, as Cx<R>
+  // OP_D2* / OP_D3*: w_k = exp(-i pi k / (2n)), k < n (DHT: (1 + i) / 2); OP_D4*:
+  // c_j = exp(-i pi j / (2n)), j < n, then d_k = exp(-i pi (2k+1) / (4n)), k < n; as Cx<R>
+  const void* d23_tab;
   int n_in, n_out;
   int lmap_tile;     // lanes along the tile dimension (tile dim contiguous in input)
   int store_direct;  // store from registers with the load mapping
@@ -172,8 +174,10 @@ __host__ __device__ constexpr int fast_pts(int logm) {
 
 // Operations of the fast pass that pack two real lines in one complex line.
 __host__ __device__ constexpr bool fast_packed(int op) {
-  return op == OP_R2C || op == OP_C2R || op == OP_X00R || op == OP_D2R || op == OP_D3R;
+  return op == OP_R2C || op == OP_C2R || op == OP_X00R || op == OP_D2R || op == OP_D3R || op == OP_D4R;
 }
+// REDFT11 / RODFT11 through one DFT of twice their length
+__host__ __device__ constexpr bool fast_d4(int op) { return op == OP_D4C || op == OP_D4R; }
 // REDFT10 / 01 and RODFT10 / 01 through one DFT of their length
 __host__ __device__ constexpr bool fast_d23(int op) {
   return op == OP_D2C || op == OP_D2R || op == OP_D3C || op == OP_D3R;
@@ -451,7 +455,7 @@ template <typename R>
 __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
   return sizeof(R) == 4 && fast_pts<R>(logm) == 16
              ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)  // 16 points: 64 registers a thread
-         : sizeof(R) == 4 && (op == OP_CSUM || fast_d23(op))
+         : sizeof(R) == 4 && (op == OP_CSUM || fast_d23(op) || fast_d4(op))
              // the sum's terms; the two loads a position of D3: ~0.2-0.5 KB of spill at 32 registers
              ? (fast_threads<R>(logm, op) >= 1024 ? 1 : 2)
          : sizeof(R) == 4
@@ -462,7 +466,7 @@ __host__ __device__ constexpr int fast_min_blocks(int logm, int op, int iom) {
                            ? (op == OP_C2R && PFGB_FAST_F32_MINBLOCKS > 3 ? 3 : PFGB_FAST_F32_MINBLOCKS)
                            : 2048 / fast_threads<R>(logm, op)))
          : fast_threads<R>(logm, op) >= 512 ? 1
-         : fast_d23(op) ? 3  // two loads a position (D3) or two real lines (D2R / D3R): ~0.2-0.5 KB of spill at 64 registers
+         : (fast_d23(op) || fast_d4(op)) ? 3  // two loads a position (D3) or two real lines (D2R / D3R): ~0.2-0.5 KB of spill at 64 registers
          : PFGB_FAST_DD_MINBLOCKS <= 0 ? 512 / fast_threads<R>(logm, op)
          : (op == OP_C2R && !(iom & 1) && PFGB_FAST_DD_MINBLOCKS > 4) ? 4
                                                                      : PFGB_FAST_DD_MINBLOCKS;
@@ -893,6 +897,62 @@ __device__ __forceinline__ void fast_tile_load(const FastArgs& a, int64_t bid, c
         v[r] = u * conj(ldg_tw<R>(a.d23_tab, b + r * T));
       }
     }
+  } else if constexpr (fast_d4(OP)) {
+    // REDFT11 / RODFT11: the M-point DFT (M = 2n) of x[pos] c_pos, pos < n
+    // (registers r < H = P / 2: pos = b + r T < H T = n), zero above (with
+    // 8 points a thread the first stage does not read registers r >= 4)
+    constexpr bool PK = OP == OP_D4R;
+    constexpr int H = P / 2;
+    Cx<R> y[H];
+    if constexpr (PK) {
+      const MR* in = reinterpret_cast<const MR*>(src) + ioff;
+      const int i0 = 2 * p, i1 = 2 * p + 1;
+      MR a0[H], a1[H];
+#pragma unroll
+      for (int r = 0; r < H; ++r) {
+        const int64_t off = (int64_t)(b + r * T) * ssa;
+        a0[r] = i0 < nvalid ? in[off + (int64_t)i0 * sst] : MR(0);
+        a1[r] = i1 < nvalid ? in[off + (int64_t)i1 * sst] : MR(0);
+      }
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < H; ++r) emx = max(emx, max(dexp_u(a0[r]), dexp_u(a1[r])));
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax_out = emax + a.emax_shift;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < H; ++r) y[r] = mk(mkr<R>(a0[r], emax), mkr<R>(a1[r], emax));
+    } else if (IO::kDD && IN_DD) {
+      const float4* in = reinterpret_cast<const float4*>(src) + ioff + (int64_t)p * sst;
+#pragma unroll
+      for (int r = 0; r < H; ++r) {
+        const int pos = b + r * T;
+        y[r] = ld_dd4<R>(p < nvalid ? in[(int64_t)pos * ssa] : make_float4(0.f, 0.f, 0.f, 0.f));
+        if (IO::kDD && a.te_rescale && p < nvalid) y[r] = scale_pow2(y[r], te_factor(a, o.tebase, t0 + p, pos, emax));
+      }
+    } else {
+      const MC* in = reinterpret_cast<const MC*>(src) + ioff + (int64_t)p * sst;
+      MC ra[H];
+#pragma unroll
+      for (int r = 0; r < H; ++r) ra[r] = p < nvalid ? in[(int64_t)(b + r * T) * ssa] : MC{0, 0};
+      if constexpr (IO::kDD) {
+        if (a.self_scale) {
+          unsigned emx = 0;
+#pragma unroll
+          for (int r = 0; r < H; ++r) emx = max(emx, max(dexp_u(ra[r].x), dexp_u(ra[r].y)));
+          emax = line_exponent<R, LOGM, OP, P>(emx, a, (unsigned)bid, t0, p, ncl_valid, a.lmap_tile != 0);
+          emax_out = emax + a.emax_shift;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < H; ++r) y[r] = mk(mkr<R>(ra[r].x, emax), mkr<R>(ra[r].y, emax));
+    }
+#pragma unroll
+    for (int r = 0; r < P; ++r)
+      v[r] = r < H ? y[r < H ? r : 0] * ldg_tw<R>(a.d23_tab, b + r * T) : mk(R(0), R(0));
   } else if constexpr (OP == OP_R2C) {
     const MR* in = reinterpret_cast<const MR*>(src) + ioff;
     const int i0 = 2 * p, i1 = 2 * p + 1;
@@ -1001,7 +1061,7 @@ __device__ __forceinline__ void fast_tile_store(const FastArgs& a, int64_t bid, 
 #pragma unroll
     for (int r = 0; r < P; ++r) v[r] = tw_mul<R, SIGN>(v[r], a.t4_tab, (int)(n1 * (int64_t)(b + r * T)));
   }
-  if (a.store_direct && OP != OP_R2C && !fast_d23(OP)) {
+  if (a.store_direct && OP != OP_R2C && !fast_d23(OP) && !fast_d4(OP)) {
     if constexpr (OP == OP_C2C || OP == OP_CSUM || OP == OP_C2CT) {
       if (p < nvalid) {
         if (IO::kDD && OUT_DD) {
@@ -1220,6 +1280,38 @@ __device__ __forceinline__ void fast_tile_store(const FastArgs& a, int64_t bid, 
         reinterpret_cast<MC*>(a.out)[ooff + off + (int64_t)q * a.out_st] = o;
       }
     }
+  } else if constexpr (fast_d4(OP)) {
+    // outputs k < n = M / 2: d_k V[k] + conj(d_k) V[M-1-k] (REDFT11), i times
+    // d_k V[k] - conj(d_k) V[M-1-k] (RODFT11); d_k at table entry n + k
+    constexpr bool PK = OP == OP_D4R;
+    constexpr int N = M / 2;
+    const int odd = a.r2r_odd;
+    const int tot = TW * N;
+    for (int e = tid; e < tot; e += nth) {
+      int q, k;
+      if (a.out_tfast) { q = e % TW; k = e / TW; } else { k = e % N; q = e / N; }
+      if (!PK && q >= nvalid) continue;
+      const Cx<R> f = z[sidx<R, LOGM, OP>(q, k)] * ldg_tw<R>(a.d23_tab, N + k);
+      const Cx<R> g = z[sidx<R, LOGM, OP>(q, M - 1 - k)] * conj(ldg_tw<R>(a.d23_tab, N + k));
+      Cx<R> y = odd ? mul_i(f - g) : f + g;
+      y = apply_scale(y, a);
+      const int64_t off = (int64_t)k * a.out_sa;
+      if constexpr (PK) {
+        MR* out = reinterpret_cast<MR*>(a.out) + ooff;
+        const int i0 = 2 * q, i1 = 2 * q + 1;
+        const int eo = line_emax_out(q);
+        if (i0 < nvalid) out[off + (int64_t)i0 * a.out_st] = outr<R>(y.re, eo);
+        if (i1 < nvalid) out[off + (int64_t)i1 * a.out_st] = outr<R>(y.im, eo);
+      } else if (IO::kDD && OUT_DD) {
+        reinterpret_cast<float4*>(a.out)[ooff + off + (int64_t)q * a.out_st] = st_dd4(y);
+      } else {
+        const int eo = line_emax_out(q);
+        MC o;
+        o.x = outr<R>(y.re, eo);
+        o.y = outr<R>(y.im, eo);
+        reinterpret_cast<MC*>(a.out)[ooff + off + (int64_t)q * a.out_st] = o;
+      }
+    }
   } else {  // C2R with a transposed output layout
     MR* out = reinterpret_cast<MR*>(a.out) + ooff;
     const int tot = TW * M;
@@ -1257,7 +1349,8 @@ __device__ __forceinline__ void fast_tile_std(const FastArgs& a, int64_t bid, Cx
   // per-line exponents of a self-scaled pass, for the stores of other lines
   __shared__ int lexp[TW];
   if (IO::kDD && a.self_scale && b == 0) lexp[p] = s.emax;
-  fast_stages<R, LOGM, SIGN, OP, P>(v, z, p, b, a.tw, a.lmap_tile != 0);
+  // (REDFT11 / RODFT11: the upper half of the DFT input is the zero padding)
+  fast_stages<R, LOGM, SIGN, OP, P, fast_d4(OP) && P == 8>(v, z, p, b, a.tw, a.lmap_tile != 0);
   fast_tile_store<R, LOGM, SIGN, OP, IOM>(a, bid, p, b, s, v, z, lexp);
 }
 

@@ -26,6 +26,11 @@ int launch_fast_dd_d2c_2(int logm, int sign, const FastArgs& A, int64_t grid, cu
 int launch_fast_dd_d3c_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_d2c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_d3c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d4c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d4c_1(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d4c_2(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d4c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_dd_d4r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_d2r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd_d3r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
@@ -62,6 +67,11 @@ int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStre
     case OP_D3C * 4 + 2: return launch_fast_dd_d3c_2(logm, sign, A, grid, s);
     case OP_D2C * 4 + 3: return launch_fast_dd_d2c_3(logm, sign, A, grid, s);
     case OP_D3C * 4 + 3: return launch_fast_dd_d3c_3(logm, sign, A, grid, s);
+    case OP_D4C * 4 + 0: return launch_fast_dd_d4c_0(logm, sign, A, grid, s);
+    case OP_D4C * 4 + 1: return launch_fast_dd_d4c_1(logm, sign, A, grid, s);
+    case OP_D4C * 4 + 2: return launch_fast_dd_d4c_2(logm, sign, A, grid, s);
+    case OP_D4C * 4 + 3: return launch_fast_dd_d4c_3(logm, sign, A, grid, s);
+    case OP_D4R * 4 + 0: return launch_fast_dd_d4r_0(logm, sign, A, grid, s);
     case OP_D2R * 4 + 0: return launch_fast_dd_d2r_0(logm, sign, A, grid, s);
     case OP_D3R * 4 + 0: return launch_fast_dd_d3r_0(logm, sign, A, grid, s);
     default: return PFGB_ERR_UNSUPPORTED;

@@ -1,5 +1,5 @@
-// Register Stockham pass, double-float (dd) arithmetic for Float64 data: REDFT10 / RODFT10 and
-// REDFT01 / RODFT01 through one DFT of their length, complex lines, dd input, dd output.
+// Register Stockham pass, double-float (dd) arithmetic for Float64 data: REDFT10 / RODFT10,
+// REDFT01 / RODFT01 and DHT through one DFT of their length, REDFT11 / RODFT11 through one of twice it, complex lines, dd input, dd output.
 #include "pfgb_fast_launch.cuh"
 
 namespace pfgb {
@@ -9,6 +9,9 @@ int launch_fast_dd_d2c_3(int logm, int sign, const FastArgs& A, int64_t grid, cu
 }
 int launch_fast_dd_d3c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   return launch_fast_op_bwd<dd, OP_D3C, 3>(logm, sign, A, grid, s);
+}
+int launch_fast_dd_d4c_3(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op_fwd<dd, OP_D4C, 3>(logm, sign, A, grid, s);
 }
 
 }  // namespace pfgb

@@ -11,5 +11,8 @@ int launch_fast_dd_d2r_0(int logm, int sign, const FastArgs& A, int64_t grid, cu
 int launch_fast_dd_d3r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   return launch_fast_op_bwd<dd, OP_D3R, 0>(logm, sign, A, grid, s);
 }
+int launch_fast_dd_d4r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
+  return launch_fast_op_fwd<dd, OP_D4R, 0>(logm, sign, A, grid, s);
+}
 
 }  // namespace pfgb

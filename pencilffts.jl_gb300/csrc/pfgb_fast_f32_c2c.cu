@@ -20,6 +20,8 @@ int launch_fast_f32_d2c_0(int logm, int sign, const FastArgs& A, int64_t grid, c
 int launch_fast_f32_d3c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_f32_d2r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_f32_d3r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_f32_d4c_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
+int launch_fast_f32_d4r_0(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s) {
   const int iom = 0;
@@ -35,6 +37,8 @@ int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStr
     case OP_D3C * 4 + 0: return launch_fast_f32_d3c_0(logm, sign, A, grid, s);
     case OP_D2R * 4 + 0: return launch_fast_f32_d2r_0(logm, sign, A, grid, s);
     case OP_D3R * 4 + 0: return launch_fast_f32_d3r_0(logm, sign, A, grid, s);
+    case OP_D4C * 4 + 0: return launch_fast_f32_d4c_0(logm, sign, A, grid, s);
+    case OP_D4R * 4 + 0: return launch_fast_f32_d4r_0(logm, sign, A, grid, s);
     default: return PFGB_ERR_UNSUPPORTED;
   }
 }

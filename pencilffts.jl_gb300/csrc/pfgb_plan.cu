@@ -671,6 +671,30 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   {
     const int n = (int)n_in;
     const bool dht = ps.r2r_kind == K_DHT;
+    // REDFT11 / RODFT11 of n points: one 2n-point DFT (4 <= n <= 2048)
+    const bool d4 = ps.r2r_kind == K_REDFT11 || ps.r2r_kind == K_RODFT11;
+    if ((ps.op == OP_R2R_C || ps.op == OP_R2R_R) && d4 && !P->fx && n >= 4 && n <= 2048 && (n & (n - 1)) == 0 &&
+        !(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+      ps.fast = true;
+      ps.fop = ps.op == OP_R2R_C ? OP_D4C : OP_D4R;
+      ps.sign = -1;
+      ps.logm = 0;
+      while ((1 << ps.logm) < 2 * n) ++ps.logm;
+      std::vector<std::complex<ld>> w(2 * (size_t)n);
+      for (int j = 0; j < n; ++j) {
+        w[j] = expi_pi(j, 2 * (int64_t)n);                   // c_j = exp(-i pi j / (2n))
+        w[n + j] = expi_pi(2 * (int64_t)j + 1, 4 * (int64_t)n);  // d_j = exp(-i pi (2j+1) / (4n))
+      }
+      int rc2 = upload_fast_table(P, 2 * n, &ps.ftw);
+      if (!rc2) rc2 = upload_fast_vec(P, "d4/" + std::to_string(n), w, &ps.d23_tab);
+      if (rc2) return rc2;
+      const bool packed = fast_packed(ps.fop);
+      ps.clines = P->rb == 8 ? fast_tw<dd>(ps.logm, ps.fop) : fast_tw<float>(ps.logm, ps.fop);
+      ps.lines = packed ? 2 * ps.clines : ps.clines;
+      ps.threads = P->rb == 8 ? fast_threads<dd>(ps.logm, ps.fop) : fast_threads<float>(ps.logm, ps.fop);
+      ps.smem = P->rb == 8 ? fast_smem<dd>(ps.logm, ps.fop) : fast_smem<float>(ps.logm, ps.fop);
+      return PFGB_OK;
+    }
     const bool d2 = ps.r2r_kind == K_REDFT10 || ps.r2r_kind == K_RODFT10 || dht;
     const bool d3 = ps.r2r_kind == K_REDFT01 || ps.r2r_kind == K_RODFT01;
     if ((ps.op == OP_R2R_C || ps.op == OP_R2R_R) && (d2 || d3) && !P->fx && n >= 8 && n <= 4096 &&
@@ -984,7 +1008,8 @@ static int make_fast_args(const pfgb_plan* P, const Pass& ps, const void* in, vo
   F.t4_tab = ps.t4_tab;
   F.t4_role = ps.t4_dim >= 0 ? pass_role(ps, ps.t4_dim) : 0;
   F.op = ps.fop;
-  F.r2r_odd = (ps.r2r_kind == K_RODFT00 || ps.r2r_kind == K_RODFT10 || ps.r2r_kind == K_RODFT01) ? 1
+  F.r2r_odd = (ps.r2r_kind == K_RODFT00 || ps.r2r_kind == K_RODFT10 || ps.r2r_kind == K_RODFT01 ||
+               ps.r2r_kind == K_RODFT11) ? 1
               : ps.r2r_kind == K_DHT                                                             ? 2
                                                                                                  : 0;
   F.d23_tab = ps.d23_tab;
@@ -2317,7 +2342,7 @@ static int plan_build(const pfgb_plan_desc* desc, pfgb_plan** out, bool query_on
       // passes that exchange dd-form data with their neighbours (packed real
       // R2R lines always read and write doubles)
       auto chains = [](const Pass& q) {
-        return q.fast && q.fop != OP_X00R && q.fop != OP_D2R && q.fop != OP_D3R && !q.four;
+        return q.fast && q.fop != OP_X00R && q.fop != OP_D2R && q.fop != OP_D3R && q.fop != OP_D4R && !q.four;
       };
       for (size_t i = 0; i < v.size(); ++i) {
         if (!v[i].fast) continue;
