@@ -684,6 +684,39 @@ struct CopyArgs {
   int real_is_double;       // element real type for scaling
 };
 
+// Real lines longer than one register pass: two real lines x1, x2 of n
+// points (neighbours along the pair dimension of the real-side layout,
+// index 2c and 2c + 1) travel as one complex line z = x1 + i x2 through an
+// n-point c2c transform; these four element maps go either side of it.
+// The complex side holds one line per pair (the pair dimension halved,
+// rounded up: the last pair of an odd count has no second line).  The two
+// layouts of a map usually share their memory order; where the c2c passes
+// cannot carry a change of order, the separating map does (strided reads).
+enum LPackMode : int {
+  LP_R2C_PACK = 0,    // x -> z[k] = x[k, 2c] + i x[k, 2c+1], k < n
+  LP_R2C_SEP = 1,     // Z -> X[k, 2c] = (Z[k] + conj Z[n-k]) / 2,
+                      //      X[k, 2c+1] = (Z[k] - conj Z[n-k]) / 2i, k <= n/2
+  LP_C2R_HPACK = 2,   // X -> Z[k] = X[k, 2c] + i X[k, 2c+1] and
+                      //      Z[n-k] = conj X[k, 2c] + i conj X[k, 2c+1], k <= n/2
+                      //      (imaginary parts at k = 0 and k = n/2 dropped)
+  LP_C2R_UNPACK = 3,  // z -> x[k, 2c] = Re z[k], x[k, 2c+1] = Im z[k], k < n
+};
+
+struct LPackArgs {
+  const void* in;
+  void* out;
+  int mode, nd;
+  int qa, qp;      // positions of the line axis and of the pair dimension (-1: none)
+  int64_t n;       // complex DFT length
+  int64_t npair;   // full extent of the pair dimension
+  int64_t total;   // iteration points (product of ext)
+  int64_t ext[kMaxOuter];  // iteration extents in memory order (fastest first)
+  int64_t ist[kMaxOuter], ost[kMaxOuter];  // strides (elements) per iteration coordinate
+  Div31 dext[kMaxOuter];   // division by ext (total < 2^31)
+  int64_t ist_a, ost_a;    // strides of the line axis
+  int64_t in_pst, out_pst; // offset of a pair's second line on the side that holds both
+};
+
 template <typename E>
 __global__ void copy_kernel(const CopyArgs a) {
   const E* in = reinterpret_cast<const E*>(a.in);

@@ -42,4 +42,108 @@ int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s) {
   return PFGB_OK;
 }
 
+// The element maps of LPackMode, one iteration point per thread (grid
+// stride), in the output's memory order.  Where both layouts share it,
+// consecutive threads touch consecutive elements on both sides, partner
+// Z[n-k] included (a descending run when the line axis is the fastest).
+template <typename R, typename C, bool BIG>
+__global__ void __launch_bounds__(256) lpack_kernel(const LPackArgs a) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = e, io = 0, oo = 0, k = 0, c = 0;
+    for (int q = 0; q < a.nd; ++q) {
+      int64_t idx;
+      if constexpr (BIG) {
+        idx = rem % a.ext[q];
+        rem /= a.ext[q];
+      } else {
+        const unsigned qq = div31((unsigned)rem, a.dext[q]);
+        idx = rem - (int64_t)qq * a.ext[q];
+        rem = qq;
+      }
+      io += idx * a.ist[q];
+      oo += idx * a.ost[q];
+      if (q == a.qa) k = idx;
+      if (q == a.qp) c = idx;
+    }
+    const bool two = a.qp >= 0 && 2 * c + 1 < a.npair;
+    switch (a.mode) {
+      case LP_R2C_PACK: {
+        const R* x = reinterpret_cast<const R*>(a.in);
+        C z;
+        z.x = x[io];
+        z.y = two ? x[io + a.in_pst] : R(0);
+        reinterpret_cast<C*>(a.out)[oo] = z;
+        break;
+      }
+      case LP_R2C_SEP: {
+        const C* Z = reinterpret_cast<const C*>(a.in);
+        C* X = reinterpret_cast<C*>(a.out);
+        const C u = Z[io];
+        const C v = Z[io + ((k ? a.n - k : 0) - k) * a.ist_a];  // Z[n-k]
+        C x1, x2;
+        x1.x = R(0.5) * (u.x + v.x);
+        x1.y = R(0.5) * (u.y - v.y);
+        X[oo] = x1;
+        if (two) {
+          x2.x = R(0.5) * (u.y + v.y);
+          x2.y = R(0.5) * (v.x - u.x);
+          X[oo + a.out_pst] = x2;
+        }
+        break;
+      }
+      case LP_C2R_HPACK: {
+        const C* X = reinterpret_cast<const C*>(a.in);
+        C* Z = reinterpret_cast<C*>(a.out);
+        C x1 = X[io], x2;
+        if (two) {
+          x2 = X[io + a.in_pst];
+        } else {
+          x2.x = R(0);
+          x2.y = R(0);
+        }
+        const bool self = k == 0 || 2 * k == a.n;  // entries of a real DFT value
+        if (self) {
+          x1.y = R(0);
+          x2.y = R(0);
+        }
+        C z;
+        z.x = x1.x - x2.y;
+        z.y = x1.y + x2.x;
+        Z[oo] = z;
+        if (!self) {
+          z.x = x1.x + x2.y;
+          z.y = x2.x - x1.y;
+          Z[oo + (a.n - 2 * k) * a.ost_a] = z;  // Z[n-k]
+        }
+        break;
+      }
+      default: {  // LP_C2R_UNPACK
+        const C z = reinterpret_cast<const C*>(a.in)[io];
+        R* x = reinterpret_cast<R*>(a.out);
+        x[oo] = z.x;
+        if (two) x[oo + a.out_pst] = z.y;
+        break;
+      }
+    }
+  }
+}
+
+int launch_lpack(int real_bytes, const LPackArgs& L, cudaStream_t s) {
+  if (L.total == 0) return PFGB_OK;
+  int64_t blocks = (L.total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  const bool big = L.total >= (int64_t{1} << 31);
+  if (real_bytes == 8) {
+    if (big) lpack_kernel<double, double2, true><<<(unsigned)blocks, 256, 0, s>>>(L);
+    else lpack_kernel<double, double2, false><<<(unsigned)blocks, 256, 0, s>>>(L);
+  } else {
+    if (big) lpack_kernel<float, float2, true><<<(unsigned)blocks, 256, 0, s>>>(L);
+    else lpack_kernel<float, float2, false><<<(unsigned)blocks, 256, 0, s>>>(L);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_cuda(e, "lpack_kernel launch");
+  return PFGB_OK;
+}
+
 }  // namespace pfgb

@@ -97,7 +97,10 @@ struct Layout {
 // ---------------------------------------------------------------------------
 // One executable pass.
 // ---------------------------------------------------------------------------
-enum PassKind { PK_TRANSFORM = 0, PK_COPY = 1 };
+// PK_LPACK: an element map either side of the c2c transform of a long real
+// line (LPackMode, lp_mode; lp_dim the pair dimension or -1, lp_n the line's
+// DFT length)
+enum PassKind { PK_TRANSFORM = 0, PK_COPY = 1, PK_LPACK = 2 };
 
 struct Pass {
   PassKind pk = PK_TRANSFORM;
@@ -166,6 +169,8 @@ struct Pass {
   int lines = 1, clines = 1, bpl = 1, lp = 0, threads = 0;
   size_t smem = 0;
   bool zero_fill = false;
+  int lp_mode = 0, lp_dim = -1;
+  int64_t lp_n = 0;
   // buffer assignment: 0 = src, 1 = dst, 2 = scratch 1, 3 = scratch 2
   int bin = 0, bout = 1;
 };
@@ -623,7 +628,7 @@ static int bluestein_form(pfgb_plan* P, Pass& ps) {
 }
 
 static int prepare_pass(pfgb_plan* P, Pass& ps) {
-  if (ps.pk == PK_COPY) {
+  if (ps.pk == PK_COPY || ps.pk == PK_LPACK) {
     ps.threads = 256;
     return PFGB_OK;
   }
@@ -774,7 +779,7 @@ static int prepare_pass(pfgb_plan* P, Pass& ps) {
   const int Lc = ps.L > 0 ? ps.L : ps.M;
   int rmin = 64;
   for (int i = 0; i < ps.nst; ++i) rmin = std::min(rmin, ps.rad[i]);
-  ps.bpl = Lc / rmin;
+  ps.bpl = std::max(1, Lc / rmin);  // a line of one point has no stage (identity)
   ps.lp = Lc;
   const bool packed = ps.op == OP_R2C || ps.op == OP_C2R || ps.op == OP_R2R_R;
   const size_t cbytes = 2 * (size_t)P->rb;
@@ -1117,10 +1122,51 @@ static int make_copy_args(const Pass& ps, const void* in, void* out, CopyArgs& C
   return PFGB_OK;
 }
 
+// Iteration space of a PK_LPACK map: the output layout's memory order, n
+// points along the axis (n / 2 + 1 for the maps on the half-spectrum side),
+// the pair dimension halved; on the side that holds both lines of a pair the
+// pair coordinate c addresses line 2c, and line 2c + 1 is in_pst / out_pst
+// further.
+static int make_lpack_args(const Pass& ps, const void* in, void* out, LPackArgs& L) {
+  std::memset(&L, 0, sizeof(L));
+  L.in = in;
+  L.out = out;
+  L.mode = ps.lp_mode;
+  L.n = ps.lp_n;
+  const int a = ps.axis, p = ps.lp_dim;
+  const bool in_pairs = ps.lp_mode == LP_R2C_PACK || ps.lp_mode == LP_C2R_HPACK;
+  const Layout& O = ps.lout;
+  const Layout& H = in_pairs ? ps.lout : ps.lin;  // one line per pair
+  const Layout& F = in_pairs ? ps.lin : ps.lout;  // both lines
+  const bool half = ps.lp_mode == LP_R2C_SEP || ps.lp_mode == LP_C2R_HPACK;
+  if (O.D > kMaxOuter) return fail(PFGB_ERR_UNSUPPORTED, "too many dimensions");
+  L.nd = O.D;
+  L.qa = L.qp = -1;
+  int64_t total = 1;
+  for (int q = 0; q < O.D; ++q) {
+    const int d = O.perm[q];
+    L.ext[q] = d == a ? (half ? ps.lp_n / 2 + 1 : ps.lp_n) : H.size[d];
+    L.ist[q] = ps.lin.stride(d) * (in_pairs && d == p ? 2 : 1);
+    L.ost[q] = ps.lout.stride(d) * (!in_pairs && d == p ? 2 : 1);
+    if (d == a) L.qa = q;
+    if (d == p) L.qp = q;
+    total *= L.ext[q];
+  }
+  L.total = total;
+  for (int q = 0; q < O.D; ++q) L.dext[q] = make_div31(L.ext[q] < (int64_t{1} << 31) ? L.ext[q] : 1);
+  L.npair = p >= 0 ? F.size[p] : 1;
+  L.ist_a = ps.lin.stride(a);
+  L.ost_a = ps.lout.stride(a);
+  L.in_pst = in_pairs && p >= 0 ? ps.lin.stride(p) : 0;
+  L.out_pst = !in_pairs && p >= 0 ? ps.lout.stride(p) : 0;
+  return PFGB_OK;
+}
+
 // Launchers (pfgb_kernels.cu)
 int launch_pass(int real_bytes, const PassArgs& A, int64_t grid, int threads, size_t smem,
                 cudaStream_t s);
 int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s);
+int launch_lpack(int real_bytes, const LPackArgs& L, cudaStream_t s);
 int launch_fast_f32(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 int launch_fast_dd(int logm, int sign, const FastArgs& A, int64_t grid, cudaStream_t s);
 
@@ -1287,12 +1333,30 @@ static bool split_layout(const Layout& L, int a, int v, int64_t m1, int64_t m2, 
   return true;
 }
 
+// Memory orders a transform pass can pair: its axis the fastest dimension on
+// one side, or both sides with the same fastest dimension (the tile
+// dimension of the pass kernels).
+static bool orders_compatible(const Layout& lin, const Layout& lout, int a) {
+  return lin.perm[0] == a || lout.perm[0] == a || lin.perm[0] == lout.perm[0];
+}
+
+// The sizes, element type and padding-free extent of `L` in the memory
+// order of `order`.
+static Layout reordered(const Layout& L, const Layout& order) {
+  Layout r = L;
+  for (int q = 0; q < L.D; ++q) r.perm[q] = order.perm[q];
+  r.pitch0 = r.size[r.perm[0]];
+  return r;
+}
+
 // Long c2c lines (M > 4096): M = M1 * M2 with M2 = 2^k (8 <= 2^k <= 4096)
 // and M1 a one-pass length, two passes: with n = n1 + M1 n2 and
 // k = k2 + M2 k1, pass A transforms n2 (the layout's dimension a split as
 // (n1 faster, n2)) and multiplies by W_M^(n1 k2); pass B transforms n1 and
 // writes X[k2 + M2 k1] through the output layout split as (k2 faster, k1).
-// Chooses the split with the most balanced M1, M2; false if none.
+// Chooses the split with the most balanced M1, M2; false if none, or if the
+// second pass's orders do not pair (an axis that is fastest on neither side
+// of a pass that changes the memory order).
 static bool split_long_pass(const Pass& ps, Pass& A, Pass& B) {
   if (ps.pk != PK_TRANSFORM || ps.op != OP_C2C) return false;
   const int a = ps.axis;
@@ -1311,6 +1375,7 @@ static bool split_long_pass(const Pass& ps, Pass& A, Pass& B) {
   Layout lin_s, lout_s;
   if (!split_layout(ps.lin, a, v, m1, m2, true, lin_s)) return false;
   if (!split_layout(ps.lout, a, v, m1, m2, false, lout_s)) return false;
+  if (!orders_compatible(lin_s, lout_s, a)) return false;
   A = ps;
   A.four = true;
   A.axis = v;
@@ -1323,6 +1388,66 @@ static bool split_long_pass(const Pass& ps, Pass& A, Pass& B) {
   B.axis = a;
   B.lin = lin_s;
   B.lout = lout_s;
+  return true;
+}
+
+// Long r2c / c2r lines (n > 4096 real points): three passes, an element map
+// that packs two real lines (neighbours along the pair dimension p) into one
+// complex line (r2c: z = x1 + i x2; c2r: Z = X1 + i X2 over the Hermitian
+// extension of both half spectra), the n-point c2c transform of the packed
+// lines (split in two by split_long_pass), and an element map that separates
+// the two spectra (r2c) or the real and imaginary parts (c2r).  The complex
+// layouts are the real-side and complex-side layouts with n points along the
+// axis and p halved, each in the memory order of the map beside it, so that
+// the c2c pass carries any re-layout.  false if the c2c transform has no split.
+static bool expand_long_real(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
+  if (ps.pk != PK_TRANSFORM || (ps.op != OP_R2C && ps.op != OP_C2R)) return false;
+  const int a = ps.axis;
+  const bool r2c = ps.op == OP_R2C;
+  const Layout& R = r2c ? ps.lin : ps.lout;  // real side
+  const Layout& X = r2c ? ps.lout : ps.lin;  // complex side (half spectra)
+  const int64_t n = R.size[a];
+  if (n <= 4096 || R.D > kMaxOuter) return false;
+  // pair dimension: the slowest other dimension of even size, else the
+  // slowest of size >= 2 (none: one line, imaginary part zero)
+  int p = -1;
+  for (int q = R.D - 1; q >= 0 && p < 0; --q)
+    if (R.perm[q] != a && R.size[R.perm[q]] >= 2 && R.size[R.perm[q]] % 2 == 0) p = R.perm[q];
+  for (int q = R.D - 1; q >= 0 && p < 0; --q)
+    if (R.perm[q] != a && R.size[R.perm[q]] >= 2) p = R.perm[q];
+  auto packed = [&](const Layout& order) {
+    Layout z = order;
+    for (int d = 0; d < z.D; ++d) z.size[d] = R.size[d];
+    z.size[a] = n;
+    if (p >= 0) z.size[p] = (R.size[p] + 1) / 2;
+    z.complex = true;
+    z.elt = X.elt;
+    z.pitch0 = z.size[z.perm[0]];
+    return z;
+  };
+  const Layout z_real = packed(R), z_cplx = packed(X);
+  c = ps;
+  c.op = OP_C2C;
+  c.sign = r2c ? -1 : 1;
+  c.lin = r2c ? z_real : z_cplx;
+  c.lout = r2c ? z_cplx : z_real;
+  Pass A, B;
+  if (!split_long_pass(c, A, B)) {
+    // the c2c passes keep one memory order; the separating map re-lays out
+    c.lout = c.lin;
+    if (!split_long_pass(c, A, B)) return false;
+  }
+  pre = ps;
+  pre.pk = PK_LPACK;
+  pre.lp_mode = r2c ? LP_R2C_PACK : LP_C2R_HPACK;
+  pre.lp_dim = p;
+  pre.lp_n = n;
+  pre.lin = ps.lin;
+  pre.lout = c.lin;
+  post = pre;
+  post.lp_mode = r2c ? LP_R2C_SEP : LP_C2R_UNPACK;
+  post.lin = c.lout;
+  post.lout = ps.lout;
   return true;
 }
 
@@ -1434,20 +1559,51 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
     for (int q = 0; q < N; ++q) sizes[q] = nsz[q];
     cplx = ncx;
   }
-  // lines longer than one register pass: two passes each
+  // lines longer than one register pass: real lines through a packed c2c
+  // transform, c2c lines in two passes each
   if (!(P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) {
+    std::vector<Pass> ex;
+    for (const Pass& ps : passes) {
+      Pass pre, c, post;
+      if (expand_long_real(ps, pre, c, post)) {
+        ex.push_back(pre);
+        ex.push_back(c);
+        ex.push_back(post);
+      } else {
+        ex.push_back(ps);
+      }
+    }
+    passes.swap(ex);
     std::vector<Pass> split;
     for (const Pass& ps : passes) {
       Pass A, B;
       if (split_long_pass(ps, A, B)) {
         split.push_back(A);
         split.push_back(B);
+        continue;
+      }
+      // orders the split cannot pair: the two passes in the input's order,
+      // then a copy into the output order
+      Pass c = ps;
+      if (ps.pk == PK_TRANSFORM && ps.op == OP_C2C) c.lout = reordered(ps.lout, ps.lin);
+      if (!ps.lin.same_order(ps.lout) && split_long_pass(c, A, B)) {
+        Pass cp;
+        cp.pk = PK_COPY;
+        cp.lin = c.lout;
+        cp.lout = ps.lout;
+        cp.axis = -1;
+        split.push_back(A);
+        split.push_back(B);
+        split.push_back(cp);
       } else {
         split.push_back(ps);
       }
     }
     passes.swap(split);
   }
+  for (const Pass& ps : passes)
+    if (ps.pk == PK_TRANSFORM && !orders_compatible(ps.lin, ps.lout, ps.axis))
+      return fail(PFGB_ERR_UNSUPPORTED, "internal: incompatible pass layouts");
   if (passes.empty()) {
     if (!P->inplace) {
       Pass c;
@@ -1483,7 +1639,8 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
         const int bi = prev, bo = asg[i];
         const Pass& ps = passes[i];
         const bool ip = ps.pk == PK_COPY ? ps.lin.same_order(ps.lout) && ps.lin.pitch0 == ps.lout.pitch0 && ps.lin.elt == ps.lout.elt
-                                         : inplace_ok(ps);
+                        : ps.pk == PK_LPACK ? false  // reads a pair's two lines, or Z[k] and Z[n-k]
+                                           : inplace_ok(ps);
         if (bi == bo && !ip) ok = false;
         need[bo] = std::max(need[bo], ps.lout.bytes());
         prev = bo;
@@ -1571,6 +1728,11 @@ static int execute(pfgb_plan* P, const Direction& dir, void* dst, const void* sr
       CopyArgs C;
       make_copy_args(ps, in, out, C);
       int rc = launch_copy(ps.lout.elt, C, s);
+      if (rc) return rc;
+    } else if (ps.pk == PK_LPACK) {
+      LPackArgs L;
+      int rc = make_lpack_args(ps, in, out, L);
+      if (!rc) rc = launch_lpack(P->rb, L, s);
       if (rc) return rc;
     } else if (ps.fast) {
       FastArgs F;
@@ -2692,9 +2854,10 @@ int pfgb_plan_get_timing(pfgb_plan* P, pfgb_pass_timing* out, int max, int* n) {
     e.pass = pass;
     const Pass& ps = (dir > 0 ? P->fwd : P->bwd).passes[pass];
     e.axis = ps.axis;
-    e.op = ps.pk == PK_COPY ? -1 : ps.op;
+    e.op = ps.pk == PK_COPY ? -1 : ps.op;  // PK_LPACK: the r2c / c2r it belongs to
     e.bytes_per_launch = ps.lin.bytes() + ps.lout.bytes();
     const char* kname = ps.pk == PK_COPY ? "copy_kernel"
+                        : ps.pk == PK_LPACK ? (P->rb == 8 ? "lpack_kernel<double>" : "lpack_kernel<float>")
                         : ps.tc ? "tc_pass<tf32x3>"
                         : ps.variant == 1 ? (P->rb == 8 ? "fast_pass_tma<dd>" : "fast_pass_tma<float>")
                         : ps.fast ? (P->rb == 4 ? "fast_pass<float>" : P->fx ? "fast_pass<fx>" : "fast_pass<dd>")

@@ -200,10 +200,21 @@ def test_fftw_flags_select_measurement():
 
 def test_long_c2c_lines_take_two_passes():
     """c2c lines above 4096 points are split in two register passes (host
-    plan query, no device); long r2c lines stay unsupported."""
+    plan query, no device)."""
     info = P.plan_query((16384,), T.FFT(), np.float64)
     assert info.n_passes_forward == 2 and info.n_passes_backward == 2
     info = P.plan_query((8, 1 << 20), T.FFT(), np.float32)
     assert info.n_passes_forward == 3
+
+
+def test_long_real_lines_take_four_passes():
+    """r2c / c2r lines above 4096 points: a pack map, the two passes of the
+    packed c2c line and a separating map (host plan query); lengths whose
+    c2c line has no split (no power-of-two factor of at least 8) beyond the
+    generic kernel's 8192-point core stay unsupported."""
+    for dims, tr, np_ in (((16384,), T.RFFT(), 4), ((8193,), T.BRFFT(16384), 4),
+                          ((5000, 6), T.RFFT(), 5), ((1 << 20,), T.RFFT(), 4)):
+        info = P.plan_query(dims, tr, np.float64)
+        assert info.n_passes_forward == np_ and info.n_passes_backward == np_, dims
     with pytest.raises(P.LibraryError):
-        P.plan_query((16384,), T.RFFT(), np.float64)
+        P.plan_query((8209,), T.RFFT(), np.float64)

@@ -5,7 +5,14 @@ and writes X[k2 + M2 k1] (reference: FFTW plans of any length,
 src/Transforms/c2c.jl:53-56).  Powers of two, 3 * 2^k and lengths whose
 other factor goes through Bluestein; 1D with extra dimensions, along
 strided axes, both output orders, in place, Float32 and double-float; each
-against the oracle."""
+against the oracle.
+
+Real lines longer than 4096 points (r2c / c2r): two real lines packed as one
+complex line z = x1 + i x2 (r2c) or Z = X1 + i X2 over both Hermitian
+extensions (c2r), the n-point c2c transform of the packed line in two
+passes, and a separating map; an odd number of lines (the last pair has no
+second line), a single line, strided and permuted axes, in place
+(reference src/Transforms/r2c.jl:83-101, src/multiarrays_r2c.jl:69-79)."""
 import numpy as np
 import pytest
 
@@ -29,10 +36,44 @@ def test_long_c2c_lines(cuda, real, n):
 @pytest.mark.parametrize("real", [F64, F32])
 def test_long_lines_in_3d_layouts(cuda, real):
     for dims, tr in (((6, 16384), T.FFT()), ((8, 9000, 4), T.FFT()),
-                     ((64, 12288), (T.RFFT(), T.FFT()))):
+                     ((64, 12288), (T.RFFT(), T.FFT())),
+                     ((6, 16384), (T.NoTransform(), T.FFT()))):
         for permute in (True, False):
             check_plan(P.PencilFFTPlan(dims, tr, real, permute_dims=permute), seed=5)
 
 
 def test_long_line_in_place(cuda):
     check_plan(P.PencilFFTPlan((16384, 5), T.FFT_(), F64), seed=6)
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+@pytest.mark.parametrize("n", [8192, 16384, 5000, 24576, 1 << 20])
+def test_long_real_lines(cuda, real, n):
+    """RFFT lines with an odd number of them (3, extra dimension), a single
+    line, and the BRFFT of n outputs as the forward transform."""
+    for dims, edims in (((n,), (3,)), ((n,), ())):
+        plan = P.PencilFFTPlan(dims, T.RFFT(), real, extra_dims=edims)
+        assert plan.info.n_passes_forward == 4
+        check_plan(plan, seed=n % 89)
+    plan = P.PencilFFTPlan((n // 2 + 1,), T.BRFFT(n), real, extra_dims=(2,))
+    assert plan.info.n_passes_forward == 4
+    check_plan(plan, seed=n % 83)
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+def test_long_real_lines_in_layouts(cuda, real):
+    """Long r2c lines in 2D / 3D plans with both output orders (the
+    separating map writes the permuted output), along a strided axis after a
+    NoTransform, and an even, odd and single count of pairs."""
+    for dims, tr in (((16384, 6), T.RFFT()), ((9000, 5, 3), T.RFFT()),
+                     ((12288, 1, 4), T.RFFT()), ((6, 16384), (T.NoTransform(), T.RFFT())),
+                     ((5, 8192, 3), (T.NoTransform(), T.RFFT(), T.FFT()))):
+        for permute in (True, False):
+            check_plan(P.PencilFFTPlan(dims, tr, real, permute_dims=permute), seed=7)
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+def test_long_real_lines_in_place(cuda, real):
+    """RFFT! on the padded in-place buffer (ManyPencilArray) with long lines."""
+    for dims in ((16384, 5), (8192, 4, 3)):
+        check_plan(P.PencilFFTPlan(dims, T.RFFT_(), real), seed=8)

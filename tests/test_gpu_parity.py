@@ -94,11 +94,13 @@ def test_rfft_even_odd(cuda, dims, tr):
     check_plan(plan)
 
 
-@pytest.mark.parametrize("dims", [(1,), (2,), (3,), (5, 1), (1, 7), (2, 3, 1)])
-def test_small_and_unit_sizes(cuda, dims):
+@pytest.mark.parametrize("real", [F64, F32])
+@pytest.mark.parametrize("dims", [(1,), (2,), (3,), (5, 1), (1, 7), (2, 3, 1), (4, 16, 1), (1, 16, 4), (4, 1, 16)])
+def test_small_and_unit_sizes(cuda, dims, real):
+    """Transforms along dimensions of one point (identity lines, no stage)."""
     for tr in (T.FFT(), T.RFFT(), T.BFFT()):
-        plan = P.PencilFFTPlan(dims, tr, F64)
-        check_plan(plan)
+        for permute in (True, False):
+            check_plan(P.PencilFFTPlan(dims, tr, real, permute_dims=permute))
 
 
 @pytest.mark.parametrize("precision", ["default", "fx", "native"])
