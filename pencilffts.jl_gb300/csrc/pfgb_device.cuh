@@ -700,6 +700,19 @@ enum LPackMode : int {
                       //      Z[n-k] = conj X[k, 2c] + i conj X[k, 2c+1], k <= n/2
                       //      (imaginary parts at k = 0 and k = n/2 dropped)
   LP_C2R_UNPACK = 3,  // z -> x[k, 2c] = Re z[k], x[k, 2c+1] = Im z[k], k < n
+  // R2R lines whose extension (m points) is longer than one pass: the
+  // extension gathered from the line (two real lines packed when `packed`),
+  // an m-point c2c transform, and the outputs read from its result, as
+  // r2r_pre / r2r_post do in shared memory (tab: exp(-i pi q / (4n)), q <= 4n + 1)
+  LP_R2R_PRE = 4,     // y -> z[j], j < m (every point written)
+  LP_R2R_POST = 5,    // Z -> y[k], k < n
+  // c2c lines of n points without a split, as a Bluestein convolution of
+  // length m (a power of two): chirp product and zero padding, the m-point
+  // transform, the product with the filter spectrum (divided by m), the
+  // inverse m-point transform, chirp product and truncation
+  LP_CHIRP_PRE = 6,   // x -> z[j] = x[j] c[j] (j < n), 0 (n <= j < m); tab = c
+  LP_MUL = 7,         // z -> z[j] f[j], j < m (in place allowed); tab = f
+  LP_CHIRP_POST = 8,  // Z -> y[k] = Z[k] c[k], k < n; tab = c
 };
 
 struct LPackArgs {
@@ -715,6 +728,10 @@ struct LPackArgs {
   Div31 dext[kMaxOuter];   // division by ext (total < 2^31)
   int64_t ist_a, ost_a;    // strides of the line axis
   int64_t in_pst, out_pst; // offset of a pair's second line on the side that holds both
+  int64_t m;               // extension / convolution length (R2R and chirp maps)
+  int kind;                // R2RKind of the R2R maps
+  int packed;              // R2R maps: the data side holds real pairs
+  const void* tab;         // complex table (element type of the plan)
 };
 
 template <typename E>

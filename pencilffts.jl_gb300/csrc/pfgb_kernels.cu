@@ -42,6 +42,19 @@ int launch_copy(int elt_bytes, const CopyArgs& C, cudaStream_t s) {
   return PFGB_OK;
 }
 
+template <typename R, typename C>
+__device__ __forceinline__ Cx<R> ldc(const void* p, int64_t i) {
+  const C v = reinterpret_cast<const C*>(p)[i];
+  return mk(v.x, v.y);
+}
+template <typename R, typename C>
+__device__ __forceinline__ void stc(void* p, int64_t i, Cx<R> v) {
+  C w;
+  w.x = v.re;
+  w.y = v.im;
+  reinterpret_cast<C*>(p)[i] = w;
+}
+
 // The element maps of LPackMode, one iteration point per thread (grid
 // stride), in the output's memory order.  Where both layouts share it,
 // consecutive threads touch consecutive elements on both sides, partner
@@ -118,11 +131,88 @@ __global__ void __launch_bounds__(256) lpack_kernel(const LPackArgs a) {
         }
         break;
       }
-      default: {  // LP_C2R_UNPACK
+      case LP_C2R_UNPACK: {
         const C z = reinterpret_cast<const C*>(a.in)[io];
         R* x = reinterpret_cast<R*>(a.out);
         x[oo] = z.x;
         if (two) x[oo + a.out_pst] = z.y;
+        break;
+      }
+      case LP_R2R_PRE: {
+        // point j of the extension from the line's points (r2r_pre, gathered)
+        const int64_t j = k, n = a.n, m = a.m, base = io - j * a.ist_a;
+        auto get = [&](int64_t i) -> Cx<R> {
+          const int64_t off = base + i * a.ist_a;
+          if (a.packed) {
+            const R* x = reinterpret_cast<const R*>(a.in);
+            return mk(x[off], two ? x[off + a.in_pst] : R(0));
+          }
+          return ldc<R, C>(a.in, off);
+        };
+        Cx<R> z = mk(R(0), R(0));
+        switch (a.kind) {
+          case K_DHT: z = get(j); break;
+          case K_REDFT00: z = get(j <= n - 1 ? j : m - j); break;
+          case K_RODFT00:
+            if (j >= 1 && j <= n) z = get(j - 1);
+            else if (j >= n + 2) z = -get(m - 1 - j);
+            break;
+          case K_REDFT10: z = j < n ? get(j) : get(2 * n - 1 - j); break;
+          case K_RODFT10: z = j < n ? get(j) : -get(2 * n - 1 - j); break;
+          case K_REDFT11:
+            z = j < n ? get(j) * ldc<R, C>(a.tab, 2 * j) : -(get(2 * n - 1 - j) * ldc<R, C>(a.tab, 2 * j));
+            break;
+          case K_RODFT11:
+            z = (j < n ? get(j) : get(2 * n - 1 - j)) * ldc<R, C>(a.tab, 2 * j);
+            break;
+          case K_REDFT01:
+            if (j < n) z = scal(get(j) * ldc<R, C>(a.tab, 2 * j), j == 0 ? R(0.5) : R(1));
+            break;
+          default:  // K_RODFT01
+            if (j >= 1 && j <= n) z = scal(mul_i(get(j - 1) * ldc<R, C>(a.tab, 2 * j)), j == n ? R(0.5) : R(1));
+            break;
+        }
+        stc<R, C>(a.out, oo, z);
+        break;
+      }
+      case LP_R2R_POST: {
+        // output k from the extension's transform (r2r_post)
+        const int64_t n = a.n, m = a.m, base = io - k * a.ist_a;
+        auto Z = [&](int64_t q) { return ldc<R, C>(a.in, base + q * a.ist_a); };
+        auto t = [&](int64_t q) { return ldc<R, C>(a.tab, q); };
+        Cx<R> y;
+        switch (a.kind) {
+          case K_DHT: {
+            const Cx<R> f = Z(k), g = Z(k == 0 ? 0 : m - k);
+            y = scal((f + g) + mul_i(f - g), R(0.5));
+            break;
+          }
+          case K_REDFT00: y = Z(k); break;
+          case K_RODFT00: y = mul_i(Z(k + 1)); break;
+          case K_REDFT10: y = t(2 * k) * Z(k); break;
+          case K_RODFT10: y = mul_i(t(2 * (k + 1)) * Z(k + 1)); break;
+          case K_REDFT11: y = t(2 * k + 1) * Z(k); break;
+          case K_RODFT11: y = mul_i(t(2 * k + 1) * Z(k)); break;
+          case K_REDFT01: y = Z(k) + Z(2 * n - 1 - k); break;
+          default: y = Z(k) - Z(2 * n - 1 - k); break;  // K_RODFT01
+        }
+        if (a.packed) {
+          R* x = reinterpret_cast<R*>(a.out);
+          x[oo] = y.re;
+          if (two) x[oo + a.out_pst] = y.im;
+        } else {
+          stc<R, C>(a.out, oo, y);
+        }
+        break;
+      }
+      case LP_CHIRP_PRE: {
+        Cx<R> z = mk(R(0), R(0));
+        if (k < a.n) z = ldc<R, C>(a.in, io) * ldc<R, C>(a.tab, k);
+        stc<R, C>(a.out, oo, z);
+        break;
+      }
+      default: {  // LP_MUL, LP_CHIRP_POST: product with the table entry of point k
+        stc<R, C>(a.out, oo, ldc<R, C>(a.in, io) * ldc<R, C>(a.tab, k));
         break;
       }
     }

@@ -97,9 +97,9 @@ struct Layout {
 // ---------------------------------------------------------------------------
 // One executable pass.
 // ---------------------------------------------------------------------------
-// PK_LPACK: an element map either side of the c2c transform of a long real
-// line (LPackMode, lp_mode; lp_dim the pair dimension or -1, lp_n the line's
-// DFT length)
+// PK_LPACK: an element map beside the c2c transform of a line longer than
+// one pass takes (LPackMode lp_mode; lp_dim the pair dimension of packed
+// real lines or -1)
 enum PassKind { PK_TRANSFORM = 0, PK_COPY = 1, PK_LPACK = 2 };
 
 struct Pass {
@@ -170,7 +170,9 @@ struct Pass {
   size_t smem = 0;
   bool zero_fill = false;
   int lp_mode = 0, lp_dim = -1;
-  int64_t lp_n = 0;
+  int64_t lp_n = 0, lp_m = 0;  // line length; extension / convolution length
+  bool lp_packed = false;      // R2R maps: two real lines per packed line
+  const void* lp_tab = nullptr;
   // buffer assignment: 0 = src, 1 = dst, 2 = scratch 1, 3 = scratch 2
   int bin = 0, bout = 1;
 };
@@ -314,8 +316,9 @@ static void host_fft_pow2(std::vector<std::complex<ld>>& x, int sign) {
   }
 }
 
-static int upload_table(pfgb_plan* P, const std::string& key,
-                        const std::vector<std::complex<ld>>& v, const void** out) {
+template <typename T>
+static int upload_table(pfgb_plan* P, const std::string& key, const std::vector<std::complex<T>>& v,
+                        const void** out) {
   if (P->query_only) {
     *out = nullptr;
     return PFGB_OK;
@@ -418,6 +421,51 @@ static int upload_fast_vec(pfgb_plan* P, const std::string& key, const std::vect
 // Bluestein tables of a length-M DFT of sign `sign` with convolution length
 // L >= 2M - 1: chirp w[j] = exp(sign i pi j^2 / M) (j < M) and the filter
 // spectrum FFT_L(b) / L of b[j] = conj(w[j]), b[L - j] = conj(w[j]).
+// Host FFT in double of a power-of-two length over a twiddle table computed
+// once (the filters of long Bluestein convolutions, up to 2^24 points, where
+// the long double form above would take minutes).
+static void host_fft_pow2_d(std::vector<std::complex<double>>& x, int sign) {
+  const size_t n = x.size();
+  std::vector<std::complex<double>> w(n / 2);
+  for (size_t k = 0; k < n / 2; ++k) {
+    const double ang = 2.0 * 3.141592653589793238 * (double)k / (double)n;
+    w[k] = std::complex<double>(std::cos(ang), sign < 0 ? -std::sin(ang) : std::sin(ang));
+  }
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(x[i], x[j]);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const size_t step = n / len;
+    for (size_t i = 0; i < n; i += len)
+      for (size_t k = 0; k < len / 2; ++k) {
+        const std::complex<double> u = x[i + k], v = x[i + k + len / 2] * w[k * step];
+        x[i + k] = u + v;
+        x[i + k + len / 2] = u - v;
+      }
+  }
+}
+
+// Tables of the long Bluestein form of an M-point c2c line of sign `sign`
+// with convolution length L: the chirp w_j = exp(sign i pi j^2 / M) (j < M)
+// and the filter spectrum DFT_L(b) / L of b_j = conj(w_j) at j and L - j.
+static void bluestein_long_tables(int64_t M, int64_t L, int sign, std::vector<std::complex<double>>& w,
+                                  std::vector<std::complex<double>>& bf) {
+  w.assign(M, {0, 0});
+  for (int64_t j = 0; j < M; ++j) {
+    const int64_t r = (j * j) % (2 * M);  // j < 2^23: no overflow
+    const double ang = 3.141592653589793238 * (double)r / (double)M;
+    w[j] = std::complex<double>(std::cos(ang), sign < 0 ? -std::sin(ang) : std::sin(ang));
+  }
+  bf.assign(L, {0, 0});
+  for (int64_t j = 0; j < M; ++j) bf[j] = std::conj(w[j]);
+  for (int64_t j = 1; j < M; ++j) bf[L - j] = std::conj(w[j]);
+  host_fft_pow2_d(bf, -1);
+  for (auto& x : bf) x /= (double)L;
+}
+
 static void bluestein_tables(int M, int L, int sign, std::vector<std::complex<ld>>& w,
                              std::vector<std::complex<ld>>& bf) {
   w.assign(M, {0, 0});
@@ -630,6 +678,34 @@ static int bluestein_form(pfgb_plan* P, Pass& ps) {
 static int prepare_pass(pfgb_plan* P, Pass& ps) {
   if (ps.pk == PK_COPY || ps.pk == PK_LPACK) {
     ps.threads = 256;
+    if (ps.pk == PK_COPY || P->query_only) return PFGB_OK;
+    const int md = ps.lp_mode;
+    if (md == LP_R2R_PRE || md == LP_R2R_POST) {
+      // exp(-i pi q / (4n)), q <= 4n + 1, in double (lines beyond one pass)
+      const std::string key = "r2rd" + std::to_string(ps.lp_n);
+      if (!P->tables.count(key)) {
+        const int64_t n = ps.lp_n;
+        std::vector<std::complex<double>> t(4 * (size_t)n + 2);
+        for (int64_t q = 0; q < 4 * n + 2; ++q) {
+          const double ang = 3.141592653589793238 * (double)(q % (8 * n)) / (4.0 * (double)n);
+          t[q] = std::complex<double>(std::cos(ang), -std::sin(ang));
+        }
+        int rc = upload_table(P, key, t, &ps.lp_tab);
+        if (rc) return rc;
+      }
+      ps.lp_tab = P->tables[key];
+    } else if (md == LP_CHIRP_PRE || md == LP_MUL || md == LP_CHIRP_POST) {
+      const std::string k = std::to_string(ps.lp_n) + (ps.sign > 0 ? "+" : "-");
+      if (!P->tables.count("lchirp" + k)) {
+        std::vector<std::complex<double>> w, bf;
+        bluestein_long_tables(ps.lp_n, ps.lp_m, ps.sign, w, bf);
+        const void* t = nullptr;
+        int rc = upload_table(P, "lchirp" + k, w, &t);
+        if (!rc) rc = upload_table(P, "lfilt" + k, bf, &t);
+        if (rc) return rc;
+      }
+      ps.lp_tab = P->tables[(md == LP_MUL ? "lfilt" : "lchirp") + k];
+    }
     return PFGB_OK;
   }
   const int a = ps.axis;
@@ -1122,32 +1198,42 @@ static int make_copy_args(const Pass& ps, const void* in, void* out, CopyArgs& C
   return PFGB_OK;
 }
 
-// Iteration space of a PK_LPACK map: the output layout's memory order, n
-// points along the axis (n / 2 + 1 for the maps on the half-spectrum side),
-// the pair dimension halved; on the side that holds both lines of a pair the
-// pair coordinate c addresses line 2c, and line 2c + 1 is in_pst / out_pst
-// further.
+// Iteration space of a PK_LPACK map: the output layout's memory order, the
+// output's points along the axis (n, n / 2 + 1 on the half-spectrum side,
+// or the extension / convolution length m), the pair dimension halved; on
+// the side that holds both lines of a pair the pair coordinate c addresses
+// line 2c, and line 2c + 1 is in_pst / out_pst further.
 static int make_lpack_args(const Pass& ps, const void* in, void* out, LPackArgs& L) {
   std::memset(&L, 0, sizeof(L));
   L.in = in;
   L.out = out;
-  L.mode = ps.lp_mode;
+  const int md = ps.lp_mode;
+  L.mode = md;
   L.n = ps.lp_n;
+  L.m = ps.lp_m;
+  L.kind = ps.r2r_kind;
+  L.packed = ps.lp_packed ? 1 : 0;
+  L.tab = ps.lp_tab;
   const int a = ps.axis, p = ps.lp_dim;
-  const bool in_pairs = ps.lp_mode == LP_R2C_PACK || ps.lp_mode == LP_C2R_HPACK;
+  // maps whose input is the user-side line (the output the packed line)
+  const bool data_in = md == LP_R2C_PACK || md == LP_C2R_HPACK || md == LP_R2R_PRE || md == LP_CHIRP_PRE;
+  const bool in_pairs = p >= 0 && data_in;
+  const bool out_pairs = p >= 0 && !data_in;
   const Layout& O = ps.lout;
-  const Layout& H = in_pairs ? ps.lout : ps.lin;  // one line per pair
-  const Layout& F = in_pairs ? ps.lin : ps.lout;  // both lines
-  const bool half = ps.lp_mode == LP_R2C_SEP || ps.lp_mode == LP_C2R_HPACK;
+  const Layout& H = data_in ? ps.lout : ps.lin;  // one line per pair
+  const Layout& F = data_in ? ps.lin : ps.lout;  // both lines
+  int64_t ka = ps.lp_n;
+  if (md == LP_R2C_SEP || md == LP_C2R_HPACK) ka = ps.lp_n / 2 + 1;
+  if (md == LP_R2R_PRE || md == LP_CHIRP_PRE || md == LP_MUL) ka = ps.lp_m;
   if (O.D > kMaxOuter) return fail(PFGB_ERR_UNSUPPORTED, "too many dimensions");
   L.nd = O.D;
   L.qa = L.qp = -1;
   int64_t total = 1;
   for (int q = 0; q < O.D; ++q) {
     const int d = O.perm[q];
-    L.ext[q] = d == a ? (half ? ps.lp_n / 2 + 1 : ps.lp_n) : H.size[d];
+    L.ext[q] = d == a ? ka : H.size[d];
     L.ist[q] = ps.lin.stride(d) * (in_pairs && d == p ? 2 : 1);
-    L.ost[q] = ps.lout.stride(d) * (!in_pairs && d == p ? 2 : 1);
+    L.ost[q] = ps.lout.stride(d) * (out_pairs && d == p ? 2 : 1);
     if (d == a) L.qa = q;
     if (d == p) L.qp = q;
     total *= L.ext[q];
@@ -1157,8 +1243,8 @@ static int make_lpack_args(const Pass& ps, const void* in, void* out, LPackArgs&
   L.npair = p >= 0 ? F.size[p] : 1;
   L.ist_a = ps.lin.stride(a);
   L.ost_a = ps.lout.stride(a);
-  L.in_pst = in_pairs && p >= 0 ? ps.lin.stride(p) : 0;
-  L.out_pst = !in_pairs && p >= 0 ? ps.lout.stride(p) : 0;
+  L.in_pst = in_pairs ? ps.lin.stride(p) : 0;
+  L.out_pst = out_pairs ? ps.lout.stride(p) : 0;
   return PFGB_OK;
 }
 
@@ -1349,6 +1435,38 @@ static Layout reordered(const Layout& L, const Layout& order) {
   return r;
 }
 
+// The power-of-two factor M2 (8 <= M2 <= 4096) of the most balanced split
+// M = M1 * M2 with M1 a one-pass length; 0 if none.
+static int64_t split_factor(int64_t M) {
+  if (M <= 4096 || M > (int64_t{1} << 24)) return 0;
+  int64_t best_m2 = 0;
+  double best = 1e9;
+  for (int64_t m2 = 8; m2 <= 4096 && m2 < M; m2 *= 2) {
+    if (M % m2 || !one_pass_length(M / m2)) continue;
+    const double d = std::fabs(std::log2((double)(M / m2)) - std::log2((double)m2));
+    if (d < best) { best = d; best_m2 = m2; }
+  }
+  return best_m2;
+}
+
+// How a c2c line of M points runs: one pass (register or generic kernel,
+// LF_ONE), split in two passes (LF_SPLIT), or as a Bluestein convolution of
+// a power-of-two length through split passes (LF_BLUESTEIN); LF_NONE beyond
+// 2^23 points without a split.
+enum LongForm { LF_NONE = -1, LF_ONE = 0, LF_SPLIT = 1, LF_BLUESTEIN = 2 };
+static int64_t bluestein_length(int64_t M) {
+  int64_t L = 1;
+  while (L < 2 * M - 1) L <<= 1;
+  return L;
+}
+static int long_c2c_form(int64_t M) {
+  if (M <= 4096) return LF_ONE;
+  if (split_factor(M)) return LF_SPLIT;
+  std::vector<int> rad;
+  if (M <= kMaxLc && factor_radices((int)M, rad)) return LF_ONE;  // the generic kernel's core
+  return bluestein_length(M) <= (int64_t{1} << 24) ? LF_BLUESTEIN : LF_NONE;
+}
+
 // Long c2c lines (M > 4096): M = M1 * M2 with M2 = 2^k (8 <= 2^k <= 4096)
 // and M1 a one-pass length, two passes: with n = n1 + M1 n2 and
 // k = k2 + M2 k1, pass A transforms n2 (the layout's dimension a split as
@@ -1361,16 +1479,9 @@ static bool split_long_pass(const Pass& ps, Pass& A, Pass& B) {
   if (ps.pk != PK_TRANSFORM || ps.op != OP_C2C) return false;
   const int a = ps.axis;
   const int64_t M = ps.lin.size[a];
-  if (M <= 4096 || M > (int64_t{1} << 24)) return false;
-  int64_t best_m2 = 0;
-  double best = 1e9;
-  for (int64_t m2 = 8; m2 <= 4096 && m2 < M; m2 *= 2) {
-    if (M % m2 || !one_pass_length(M / m2)) continue;
-    const double d = std::fabs(std::log2((double)(M / m2)) - std::log2((double)m2));
-    if (d < best) { best = d; best_m2 = m2; }
-  }
-  if (!best_m2) return false;
-  const int64_t m2 = best_m2, m1 = M / m2;
+  const int64_t m2 = split_factor(M);
+  if (!m2) return false;
+  const int64_t m1 = M / m2;
   const int v = ps.lin.D;  // the split's second dimension
   Layout lin_s, lout_s;
   if (!split_layout(ps.lin, a, v, m1, m2, true, lin_s)) return false;
@@ -1391,15 +1502,40 @@ static bool split_long_pass(const Pass& ps, Pass& A, Pass& B) {
   return true;
 }
 
-// Long r2c / c2r lines (n > 4096 real points): three passes, an element map
-// that packs two real lines (neighbours along the pair dimension p) into one
-// complex line (r2c: z = x1 + i x2; c2r: Z = X1 + i X2 over the Hermitian
-// extension of both half spectra), the n-point c2c transform of the packed
-// lines (split in two by split_long_pass), and an element map that separates
-// the two spectra (r2c) or the real and imaginary parts (c2r).  The complex
-// layouts are the real-side and complex-side layouts with n points along the
-// axis and p halved, each in the memory order of the map beside it, so that
-// the c2c pass carries any re-layout.  false if the c2c transform has no split.
+// Pair dimension of packed real lines along axis a: the slowest other
+// dimension of even size, else the slowest of size >= 2 (-1: one line).
+static int pair_dim(const Layout& R, int a) {
+  for (int q = R.D - 1; q >= 0; --q)
+    if (R.perm[q] != a && R.size[R.perm[q]] >= 2 && R.size[R.perm[q]] % 2 == 0) return R.perm[q];
+  for (int q = R.D - 1; q >= 0; --q)
+    if (R.perm[q] != a && R.size[R.perm[q]] >= 2) return R.perm[q];
+  return -1;
+}
+
+// The packed complex lines of a long-line form: the sizes of `data` (axis a
+// at m points, pair dimension p halved) in the memory order of `order`,
+// complex elements of elt bytes, no padding.
+static Layout packed_layout(const Layout& data, const Layout& order, int a, int64_t m, int p, int elt) {
+  Layout z = order;
+  for (int d = 0; d < z.D; ++d) z.size[d] = data.size[d];
+  z.size[a] = m;
+  if (p >= 0) z.size[p] = (data.size[p] + 1) / 2;
+  z.complex = true;
+  z.elt = elt;
+  z.pitch0 = z.size[z.perm[0]];
+  return z;
+}
+
+// Long r2c / c2r lines (n > 4096 real points whose n-point c2c line is
+// split or runs as a Bluestein convolution): an element map that packs two
+// real lines (neighbours along the pair dimension) into one complex line
+// (r2c: z = x1 + i x2; c2r: Z = X1 + i X2 over the Hermitian extension of
+// both half spectra), the n-point c2c transform of the packed lines, and an
+// element map that separates the two spectra (r2c) or the real and imaginary
+// parts (c2r).  The packed layouts take the memory order of the map beside
+// them, so that a split c2c transform carries any re-layout; where its passes
+// cannot (or for a Bluestein form) the c2c lines keep one order and the
+// separating map re-lays out.
 static bool expand_long_real(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
   if (ps.pk != PK_TRANSFORM || (ps.op != OP_R2C && ps.op != OP_C2R)) return false;
   const int a = ps.axis;
@@ -1407,36 +1543,17 @@ static bool expand_long_real(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
   const Layout& R = r2c ? ps.lin : ps.lout;  // real side
   const Layout& X = r2c ? ps.lout : ps.lin;  // complex side (half spectra)
   const int64_t n = R.size[a];
-  if (n <= 4096 || R.D > kMaxOuter) return false;
-  // pair dimension: the slowest other dimension of even size, else the
-  // slowest of size >= 2 (none: one line, imaginary part zero)
-  int p = -1;
-  for (int q = R.D - 1; q >= 0 && p < 0; --q)
-    if (R.perm[q] != a && R.size[R.perm[q]] >= 2 && R.size[R.perm[q]] % 2 == 0) p = R.perm[q];
-  for (int q = R.D - 1; q >= 0 && p < 0; --q)
-    if (R.perm[q] != a && R.size[R.perm[q]] >= 2) p = R.perm[q];
-  auto packed = [&](const Layout& order) {
-    Layout z = order;
-    for (int d = 0; d < z.D; ++d) z.size[d] = R.size[d];
-    z.size[a] = n;
-    if (p >= 0) z.size[p] = (R.size[p] + 1) / 2;
-    z.complex = true;
-    z.elt = X.elt;
-    z.pitch0 = z.size[z.perm[0]];
-    return z;
-  };
-  const Layout z_real = packed(R), z_cplx = packed(X);
+  const int form = long_c2c_form(n);
+  if (n <= 4096 || R.D > kMaxOuter || (form != LF_SPLIT && form != LF_BLUESTEIN)) return false;
+  const int p = pair_dim(R, a);
+  const Layout z_real = packed_layout(R, R, a, n, p, X.elt), z_cplx = packed_layout(R, X, a, n, p, X.elt);
   c = ps;
   c.op = OP_C2C;
   c.sign = r2c ? -1 : 1;
   c.lin = r2c ? z_real : z_cplx;
   c.lout = r2c ? z_cplx : z_real;
   Pass A, B;
-  if (!split_long_pass(c, A, B)) {
-    // the c2c passes keep one memory order; the separating map re-lays out
-    c.lout = c.lin;
-    if (!split_long_pass(c, A, B)) return false;
-  }
+  if (form == LF_BLUESTEIN || !split_long_pass(c, A, B)) c.lout = c.lin;
   pre = ps;
   pre.pk = PK_LPACK;
   pre.lp_mode = r2c ? LP_R2C_PACK : LP_C2R_HPACK;
@@ -1448,6 +1565,91 @@ static bool expand_long_real(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
   post.lp_mode = r2c ? LP_R2C_SEP : LP_C2R_UNPACK;
   post.lin = c.lout;
   post.lout = ps.lout;
+  return true;
+}
+
+// Extension length of an R2R line of n points (the generic kernel's DFT).
+static int64_t r2r_extension(int kind, int64_t n) {
+  switch (kind) {
+    case K_DHT: return n;
+    case K_REDFT00: return 2 * (n - 1);
+    case K_RODFT00: return 2 * (n + 1);
+    default: return 2 * n;
+  }
+}
+
+// R2R lines whose extension (m points) is beyond the generic kernel's core:
+// the extension gathered into packed complex lines (two real lines per
+// complex line for real data: every kind has a real kernel), the m-point c2c
+// transform (split, or Bluestein), and the outputs read from it.
+static bool expand_long_r2r(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
+  if (ps.pk != PK_TRANSFORM || (ps.op != OP_R2R_C && ps.op != OP_R2R_R)) return false;
+  const int a = ps.axis;
+  const int64_t n = ps.lin.size[a];
+  if (n < 2 || ps.lin.D > kMaxOuter) return false;
+  const int64_t m = r2r_extension(ps.r2r_kind, n);
+  std::vector<int> rad;
+  const bool generic = m <= kMaxLc && (factor_radices((int)m, rad) || bluestein_length(m) <= kMaxLc);
+  const int form = long_c2c_form(m);
+  if (generic || (form != LF_SPLIT && form != LF_BLUESTEIN)) return false;
+  const bool real = ps.op == OP_R2R_R;
+  const int p = real ? pair_dim(ps.lin, a) : -1;
+  const int celt = real ? 2 * ps.lin.elt : ps.lin.elt;
+  const Layout z = packed_layout(ps.lin, ps.lin, a, m, p, celt);
+  c = ps;
+  c.op = OP_C2C;
+  c.sign = -1;
+  c.r2r_kind = 0;
+  c.lin = c.lout = z;
+  pre = ps;
+  pre.pk = PK_LPACK;
+  pre.lp_mode = LP_R2R_PRE;
+  pre.lp_dim = p;
+  pre.lp_n = n;
+  pre.lp_m = m;
+  pre.lp_packed = real;
+  pre.lin = ps.lin;
+  pre.lout = z;
+  post = pre;
+  post.lp_mode = LP_R2R_POST;
+  post.lin = z;
+  post.lout = ps.lout;
+  return true;
+}
+
+// c2c lines of M points without a split beyond the generic kernel's core:
+// Bluestein with a power-of-two convolution length L >= 2M - 1 as element
+// maps and two split L-point transforms, chirp product and zero padding,
+// forward transform, product with the filter spectrum, inverse transform,
+// chirp product and truncation (the output map re-lays out).
+static bool expand_bluestein(const Pass& ps, std::vector<Pass>& out) {
+  if (ps.pk != PK_TRANSFORM || ps.op != OP_C2C || ps.four) return false;
+  const int a = ps.axis;
+  const int64_t M = ps.lin.size[a];
+  if (long_c2c_form(M) != LF_BLUESTEIN || ps.lin.D > kMaxOuter) return false;
+  const int64_t L = bluestein_length(M);
+  const Layout z = packed_layout(ps.lin, ps.lin, a, L, -1, ps.lin.elt);
+  Pass m = ps;
+  m.pk = PK_LPACK;
+  m.lp_dim = -1;
+  m.lp_n = M;
+  m.lp_m = L;
+  Pass pre = m, mul = m, post = m;
+  pre.lp_mode = LP_CHIRP_PRE;
+  pre.lout = z;
+  mul.lp_mode = LP_MUL;
+  mul.lin = mul.lout = z;
+  post.lp_mode = LP_CHIRP_POST;
+  post.lin = z;
+  Pass f = ps, b = ps;
+  f.lin = f.lout = b.lin = b.lout = z;
+  f.sign = -1;
+  b.sign = 1;
+  out.push_back(pre);
+  out.push_back(f);
+  out.push_back(mul);
+  out.push_back(b);
+  out.push_back(post);
   return true;
 }
 
@@ -1565,7 +1767,7 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
     std::vector<Pass> ex;
     for (const Pass& ps : passes) {
       Pass pre, c, post;
-      if (expand_long_real(ps, pre, c, post)) {
+      if (expand_long_real(ps, pre, c, post) || expand_long_r2r(ps, pre, c, post)) {
         ex.push_back(pre);
         ex.push_back(c);
         ex.push_back(post);
@@ -1573,6 +1775,10 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
         ex.push_back(ps);
       }
     }
+    passes.swap(ex);
+    ex.clear();
+    for (const Pass& ps : passes)
+      if (!expand_bluestein(ps, ex)) ex.push_back(ps);
     passes.swap(ex);
     std::vector<Pass> split;
     for (const Pass& ps : passes) {
@@ -1626,11 +1832,16 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
     int64_t best_cost = -1;
     std::vector<int> best;
     std::vector<int> asg(mm);
+    // every assignment up to 12 passes; beyond (long lines in several
+    // dimensions) the two scratch buffers alternate
     int64_t combos = 1;
-    for (int i = 0; i < mm - 1; ++i) combos *= 3;
+    for (int i = 0; i < mm - 1 && mm <= 12; ++i) combos *= 3;
     for (int64_t c = 0; c < combos; ++c) {
       int64_t cc = c;
-      for (int i = 0; i < mm - 1; ++i) { asg[i] = 1 + (int)(cc % 3); cc /= 3; }
+      for (int i = 0; i < mm - 1; ++i) {
+        asg[i] = mm <= 12 ? 1 + (int)(cc % 3) : 2 + (i & 1);
+        cc /= 3;
+      }
       asg[mm - 1] = 1;
       bool ok = true;
       int64_t need[4] = {0, 0, 0, 0};
@@ -1639,7 +1850,8 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
         const int bi = prev, bo = asg[i];
         const Pass& ps = passes[i];
         const bool ip = ps.pk == PK_COPY ? ps.lin.same_order(ps.lout) && ps.lin.pitch0 == ps.lout.pitch0 && ps.lin.elt == ps.lout.elt
-                        : ps.pk == PK_LPACK ? false  // reads a pair's two lines, or Z[k] and Z[n-k]
+                        : ps.pk == PK_LPACK ? ps.lp_mode == LP_MUL  // the others read a pair's two
+                                                                  // lines, Z[k] and Z[n-k], or change length
                                            : inplace_ok(ps);
         if (bi == bo && !ip) ok = false;
         need[bo] = std::max(need[bo], ps.lout.bytes());

@@ -207,14 +207,19 @@ def test_long_c2c_lines_take_two_passes():
     assert info.n_passes_forward == 3
 
 
-def test_long_real_lines_take_four_passes():
-    """r2c / c2r lines above 4096 points: a pack map, the two passes of the
-    packed c2c line and a separating map (host plan query); lengths whose
-    c2c line has no split (no power-of-two factor of at least 8) beyond the
-    generic kernel's 8192-point core stay unsupported."""
+def test_long_lines_pass_counts():
+    """Host plan query of lines beyond one pass: r2c / c2r lines above 4096
+    points as a pack map, the two passes of the packed c2c line and a
+    separating map; c2c lines without a split as a Bluestein convolution
+    (chirp map, two split transforms, filter product, chirp map; r2c lines
+    add their pack and separating maps); R2R lines as a gathering map, the
+    extension's c2c passes and an output map.  Beyond 2^23 points without a
+    split a line stays unsupported."""
     for dims, tr, np_ in (((16384,), T.RFFT(), 4), ((8193,), T.BRFFT(16384), 4),
-                          ((5000, 6), T.RFFT(), 5), ((1 << 20,), T.RFFT(), 4)):
+                          ((5000, 6), T.RFFT(), 5), ((1 << 20,), T.RFFT(), 4),
+                          ((8209,), T.FFT(), 7), ((8209,), T.RFFT(), 9),
+                          ((5000,), T.R2R(T.REDFT10), 4), ((4099,), T.R2R(T.REDFT11), 9)):
         info = P.plan_query(dims, tr, np.float64)
         assert info.n_passes_forward == np_ and info.n_passes_backward == np_, dims
     with pytest.raises(P.LibraryError):
-        P.plan_query((8209,), T.RFFT(), np.float64)
+        P.plan_query(((1 << 23) + 9,), T.FFT(), np.float64)

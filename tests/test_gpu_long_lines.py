@@ -12,7 +12,13 @@ complex line z = x1 + i x2 (r2c) or Z = X1 + i X2 over both Hermitian
 extensions (c2r), the n-point c2c transform of the packed line in two
 passes, and a separating map; an odd number of lines (the last pair has no
 second line), a single line, strided and permuted axes, in place
-(reference src/Transforms/r2c.jl:83-101, src/multiarrays_r2c.jl:69-79)."""
+(reference src/Transforms/r2c.jl:83-101, src/multiarrays_r2c.jl:69-79).
+
+Lengths without a split (no power-of-two factor of at least 8 with a
+one-pass cofactor) beyond the generic kernel's core run as a Bluestein
+convolution through two split power-of-two transforms; R2R lines whose
+extension is beyond that core gather the extension into packed complex lines
+around one long c2c transform (reference src/Transforms/r2r.jl:5-131)."""
 import numpy as np
 import pytest
 
@@ -77,3 +83,42 @@ def test_long_real_lines_in_place(cuda, real):
     """RFFT! on the padded in-place buffer (ManyPencilArray) with long lines."""
     for dims in ((16384, 5), (8192, 4, 3)):
         check_plan(P.PencilFFTPlan(dims, T.RFFT_(), real), seed=8)
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+@pytest.mark.parametrize("n", [4097, 8209, 100003])
+def test_long_c2c_bluestein(cuda, real, n):
+    """Prime and two-prime lengths: chirp map, split forward transform,
+    filter product, split inverse transform, chirp map."""
+    for tr in (T.FFT(), T.BFFT()):
+        plan = P.PencilFFTPlan((n,), tr, real, extra_dims=(2,))
+        assert plan.info.n_passes_forward == 7
+        check_plan(plan, seed=n % 79)
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+def test_long_real_bluestein(cuda, real):
+    """r2c / c2r lines whose packed c2c line takes the Bluestein form, in 1D
+    (odd number of lines), 2D with both output orders, and the BRFFT of an
+    odd output length."""
+    check_plan(P.PencilFFTPlan((8209,), T.RFFT(), real, extra_dims=(3,)), seed=3)
+    for permute in (True, False):
+        check_plan(P.PencilFFTPlan((8209, 4), T.RFFT(), real, permute_dims=permute), seed=4)
+    check_plan(P.PencilFFTPlan((4105,), T.BRFFT(8209), real, extra_dims=(2,)), seed=5)
+
+
+# per kind: (extension with a split, extension through Bluestein)
+R2R_LONG = {T.DHT: (9000, 8209), T.REDFT00: (8193, 8194), T.RODFT00: (8191, 8190),
+            T.REDFT10: (5000, 4099), T.REDFT01: (5000, 4099), T.REDFT11: (5000, 4099),
+            T.RODFT10: (5000, 4099), T.RODFT01: (5000, 4099), T.RODFT11: (5000, 4099)}
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+@pytest.mark.parametrize("kind", list(R2R_LONG), ids=lambda k: repr(T.R2R(k)))
+def test_long_r2r_lines(cuda, real, kind):
+    """R2R lines with an extension beyond one pass: real lines (packed in
+    pairs, an odd count) and complex lines after an FFT, both output orders."""
+    for n in R2R_LONG[kind]:
+        check_plan(P.PencilFFTPlan((n,), T.R2R(kind), real, extra_dims=(3,)), seed=n % 71)
+        for permute in (True, False):
+            check_plan(P.PencilFFTPlan((4, n), (T.FFT(), T.R2R(kind)), real, permute_dims=permute), seed=n % 67)
