@@ -50,7 +50,7 @@ def parse():
                     help="approximate CPU seconds for the cpu_baseline sample")
     ap.add_argument("--configs", default="all",
                     help="other benchmark configurations to measure after the headline: "
-                         "'all', 'none' or a comma list of C1,C2a,C2b,C3,C4,C5")
+                         "'all', 'none' or a comma list of C1,C2a,C2b,C3,C4,C5,long_lines")
     ap.add_argument("--config-steps", type=int, default=10)
     ap.add_argument("--profile-batch", action="store_true",
                     help="for ncu: build the 64 uneven Float32 fields of configuration C5, launch the batch "
@@ -677,8 +677,29 @@ def config_c5(P, O, steps, warmup):
     return out
 
 
+def config_long_lines(P, O, steps, warmup):
+    """Lines beyond one register pass: a long r2c axis (packed pair of real
+    lines, split c2c transform, separating map) and a prime c2c length
+    (Bluestein convolution through split power-of-two transforms)."""
+    import numpy as np
+    rng = np.random.default_rng(11)
+    dims = (16384, 4096)
+    x = rng.standard_normal(dims)
+    out = {"rfft_16384x4096_f64": _round_trip_config(
+        P, O, steps, warmup, dims, P.Transforms.RFFT(), np.float64, x,
+        "RFFT round trip 16384x4096 Float64 (16384-point r2c lines)", "N(0,1), seed 11 (537 MB arrays)",
+        _flop_r2c(np.prod(dims)))}
+    dims = (8209, 1024)
+    x = rng.standard_normal(dims) + 1j * rng.standard_normal(dims)
+    out["fft_8209x1024_f64"] = _round_trip_config(
+        P, O, steps, warmup, dims, P.Transforms.FFT(), np.float64, x,
+        "FFT + BFFT round trip 8209x1024 ComplexF64 (prime 8209-point lines, Bluestein)",
+        "N(0,1) real and imaginary parts, seed 11 (134 MB arrays)", _flop_c2c(np.prod(dims)))
+    return out
+
+
 CONFIGS = {"C1": config_c1, "C2a": config_c2a, "C2b": config_c2b, "C3": config_c3,
-           "C4": config_c4, "C5": config_c5}
+           "C4": config_c4, "C5": config_c5, "long_lines": config_long_lines}
 
 
 # ---------------------------------------------------------------------------
