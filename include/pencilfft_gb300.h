@@ -90,10 +90,15 @@ typedef struct pfgb_plan_desc {
  *             two), 3 * 2^k and 5 * 2^k points, and any other length up to
  *             2048 (Bluestein), REDFT00 / RODFT00 lines of 2^k +- 1 points
  *             and REDFT10 / REDFT01 / RODFT10 / RODFT01 / DHT / REDFT11 /
- *             RODFT11 lines of 2^k points;
- *             the remaining lines (other R2R kinds and lengths, longer lines)
- *             in native FP64.  Both meet a relative L2 error of
- *             1e-13.
+ *             RODFT11 lines of 2^k points, and every line beyond one pass
+ *             (c2c lines split in two passes, r2c / c2r lines as two real
+ *             lines packed in one c2c line, lines without a split as a
+ *             Bluestein convolution, R2R lines through their extension:
+ *             double-float transforms between element maps in FP64);
+ *             the remaining lines (other R2R lengths whose extension fits
+ *             the generic kernel's 8192-point core, c2c / r2c / c2r lines of
+ *             4097 .. 8192 points without a split) in native FP64.  Both
+ *             meet a relative L2 error of 1e-13.
  *   NATIVE:   Float64 plans compute every line in native FP64 (GB300's FP64
  *             rate is about 1/70 of its FP32 rate).
  *   TC_SPLIT: Float32 plans only: c2c lines of 256, 512 and 1024 points run
