@@ -1578,11 +1578,33 @@ static int64_t r2r_extension(int kind, int64_t n) {
   }
 }
 
-// R2R lines whose extension (m points) is beyond the generic kernel's core:
-// the extension gathered into packed complex lines (two real lines per
-// complex line for real data: every kind has a real kernel), the m-point c2c
-// transform (split, or Bluestein), and the outputs read from it.
-static bool expand_long_r2r(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
+// R2R kinds and lengths with a register-pass form of their own (prepare_pass:
+// REDFT00 / RODFT00 through a power-of-two extension, the D2 / D3 / DHT
+// kinds of 2^k points, REDFT11 / RODFT11 of 2^k points up to 2048).
+static bool r2r_register_form(const pfgb_plan* P, int kind, int64_t n) {
+  if (P->fx || (P->rb == 8 && P->precision == PFGB_PRECISION_NATIVE)) return false;
+  auto pow2 = [](int64_t v) { return v > 0 && (v & (v - 1)) == 0; };
+  switch (kind) {
+    case K_REDFT00:
+    case K_RODFT00: {
+      const int64_t m = r2r_extension(kind, n);
+      return pow2(m) && m >= 8 && m <= 4096;
+    }
+    case K_REDFT11:
+    case K_RODFT11: return pow2(n) && n >= 4 && n <= 2048;
+    default: return pow2(n) && n >= 8 && n <= 4096;
+  }
+}
+
+// R2R lines through their extension (m points) as a c2c line: the extension
+// gathered into packed complex lines (two real lines per complex line for
+// real data: every kind has a real kernel), the m-point c2c transform, and
+// the outputs read from it.  Taken where the extension is beyond the generic
+// kernel's core (split or Bluestein c2c), and in Float64 plans for every line
+// without a register form of its own whose extension is a one-pass length:
+// the c2c pass then runs in double-float on a register kernel instead of the
+// generic kernel's native FP64.
+static bool expand_long_r2r(const pfgb_plan* P, const Pass& ps, Pass& pre, Pass& c, Pass& post) {
   if (ps.pk != PK_TRANSFORM || (ps.op != OP_R2R_C && ps.op != OP_R2R_R)) return false;
   const int a = ps.axis;
   const int64_t n = ps.lin.size[a];
@@ -1591,7 +1613,8 @@ static bool expand_long_r2r(const Pass& ps, Pass& pre, Pass& c, Pass& post) {
   std::vector<int> rad;
   const bool generic = m <= kMaxLc && (factor_radices((int)m, rad) || bluestein_length(m) <= kMaxLc);
   const int form = long_c2c_form(m);
-  if (generic || (form != LF_SPLIT && form != LF_BLUESTEIN)) return false;
+  const bool dd_route = P->rb == 8 && !P->fx && !r2r_register_form(P, ps.r2r_kind, n) && one_pass_length(m);
+  if (!dd_route && (generic || (form != LF_SPLIT && form != LF_BLUESTEIN))) return false;
   const bool real = ps.op == OP_R2R_R;
   const int p = real ? pair_dim(ps.lin, a) : -1;
   const int celt = real ? 2 * ps.lin.elt : ps.lin.elt;
@@ -1767,7 +1790,7 @@ static int build_direction(pfgb_plan* P, bool forward, Direction& dir, int64_t c
     std::vector<Pass> ex;
     for (const Pass& ps : passes) {
       Pass pre, c, post;
-      if (expand_long_real(ps, pre, c, post) || expand_long_r2r(ps, pre, c, post)) {
+      if (expand_long_real(ps, pre, c, post) || expand_long_r2r(P, ps, pre, c, post)) {
         ex.push_back(pre);
         ex.push_back(c);
         ex.push_back(post);
