@@ -94,10 +94,12 @@ typedef struct pfgb_plan_desc {
  *             (c2c lines split in two passes, r2c / c2r lines as two real
  *             lines packed in one c2c line, lines without a split as a
  *             Bluestein convolution, R2R lines through their extension:
- *             double-float transforms between element maps in FP64);
- *             the remaining lines (other R2R lengths whose extension fits
- *             the generic kernel's 8192-point core, c2c / r2c / c2r lines of
- *             4097 .. 8192 points without a split) in native FP64.  Both
+ *             double-float transforms between element maps in FP64), and
+ *             the other R2R lines whose extension is a one-pass length
+ *             (a double-float c2c pass of the extension between element
+ *             maps); the remaining lines (R2R extensions and c2c / r2c / c2r
+ *             lines of 2049 .. 8192 points that are neither a power of two,
+ *             3 * 2^k nor 5 * 2^k and have no split) in native FP64.  Both
  *             meet a relative L2 error of 1e-13.
  *   NATIVE:   Float64 plans compute every line in native FP64 (GB300's FP64
  *             rate is about 1/70 of its FP32 rate).
