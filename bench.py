@@ -756,16 +756,19 @@ def run_gpu(args, rank, world, local_rank):
     plan.set_timing(True)
     barrier()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
+    # one event between consecutive steps: the spread of the step times
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
         step()
-    e1.record(stream)
+        evs[i + 1].record(stream)
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
-    ms_total = e0.elapsed_time(e1)
+    ms_total = evs[0].elapsed_time(evs[-1])
+    per_step = np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)])
+    step_stats = {"mean": float(per_step.mean()), "std": float(per_step.std()),
+                  "min": float(per_step.min()), "max": float(per_step.max()), "n": int(args.steps)}
     timing = plan.get_timing()
     plan.set_timing(False)
     ms_step = max_over_ranks(ms_total / args.steps, world, dev)
@@ -903,7 +906,7 @@ def run_gpu(args, rank, world, local_rank):
             torch.cuda.empty_cache()
     line = {
         "metric": METRIC, "value": ms_step, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "step_ms": step_stats,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if rb == 8 else "f32", "data": "synthetic: uniform [-1,1), seeded",
         "config": headline_config(args, world),

@@ -223,3 +223,6 @@ def test_long_lines_pass_counts():
         assert info.n_passes_forward == np_ and info.n_passes_backward == np_, dims
     with pytest.raises(P.LibraryError):
         P.plan_query(((1 << 23) + 9,), T.FFT(), np.float64)
+    # more than 12 passes: the scratch buffers alternate (no exhaustive search)
+    info = P.plan_query((4097, 4099), T.FFT(), np.float32)
+    assert info.n_passes_forward == 14 and info.scratch_bytes > 0

@@ -122,3 +122,16 @@ def test_long_r2r_lines(cuda, real, kind):
         check_plan(P.PencilFFTPlan((n,), T.R2R(kind), real, extra_dims=(3,)), seed=n % 71)
         for permute in (True, False):
             check_plan(P.PencilFFTPlan((4, n), (T.FFT(), T.R2R(kind)), real, permute_dims=permute), seed=n % 67)
+
+
+@pytest.mark.parametrize("real", [F64, F32])
+def test_many_pass_plan_and_in_place_r2r(cuda, real):
+    """A plan of more than 12 passes (Bluestein lines along both axes: the
+    scratch buffers alternate) with both output orders, and in-place R2R!
+    lines whose extension is beyond one pass."""
+    for permute in (True, False):
+        plan = P.PencilFFTPlan((4097, 4099), T.FFT(), real, permute_dims=permute)
+        assert plan.info.n_passes_forward == 14
+        check_plan(plan, seed=9)
+    check_plan(P.PencilFFTPlan((8193, 3), T.R2R_(T.REDFT00), real), seed=10)
+    check_plan(P.PencilFFTPlan((5000, 4), T.R2R_(T.RODFT10), real), seed=11)
