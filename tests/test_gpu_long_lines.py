@@ -135,3 +135,36 @@ def test_many_pass_plan_and_in_place_r2r(cuda, real):
         check_plan(plan, seed=9)
     check_plan(P.PencilFFTPlan((8193, 3), T.R2R_(T.REDFT00), real), seed=10)
     check_plan(P.PencilFFTPlan((5000, 4), T.R2R_(T.RODFT10), real), seed=11)
+
+
+def test_long_lines_in_a_batch(cuda):
+    """Long-line plans recorded into a batch: the graph form replays the
+    element maps with the passes; the persistent form has no tile for them
+    (LibraryError), and "auto" falls back to the graph form."""
+    import torch
+    from helpers import oracle_plan, rel
+    plans = [P.PencilFFTPlan((16384, 3), T.RFFT(), F32), P.PencilFFTPlan((8209,), T.FFT(), F32, extra_dims=(2,))]
+    rng = np.random.default_rng(12)
+    us = [p.allocate_input() for p in plans]
+    vs = [p.allocate_output() for p in plans]
+    ws = [p.allocate_input() for p in plans]
+    xs = []
+    for p, u in zip(plans, us):
+        x = rng.standard_normal(tuple(p.size_global_in) + tuple(p.extra_dims))
+        if np.dtype(p.eltype_input()).kind == "c":
+            x = x + 1j * rng.standard_normal(x.shape)
+        u.copy_from_logical(x)
+        xs.append(x)
+    ops = [(P.mul_, v, p, u) for p, u, v in zip(plans, us, vs)] + \
+          [(P.ldiv_, w, p, v) for p, v, w in zip(plans, vs, ws)]
+    with pytest.raises(P.LibraryError):
+        P.Batch(ops, form="persistent")
+    for form in ("graph", "auto"):
+        b = P.Batch(ops, form=form)
+        assert b.form == "graph"
+        b.launch()
+        torch.cuda.synchronize()
+        for p, x, v, w in zip(plans, xs, vs, ws):
+            assert rel(v.to_logical(), oracle_plan(p).forward(x)) <= 1e-5
+            assert rel(w.to_logical(), x) <= 1e-5
+        assert b.status() == 0
