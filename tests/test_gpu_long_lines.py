@@ -117,11 +117,11 @@ R2R_LONG = {T.DHT: (9000, 8209), T.REDFT00: (8193, 8194), T.RODFT00: (8191, 8190
 @pytest.mark.parametrize("kind", list(R2R_LONG), ids=lambda k: repr(T.R2R(k)))
 def test_long_r2r_lines(cuda, real, kind):
     """R2R lines with an extension beyond one pass: real lines (packed in
-    pairs, an odd count) and complex lines after an FFT, both output orders."""
-    for n in R2R_LONG[kind]:
+    pairs, an odd count) and complex lines after an FFT, one output order per
+    length (both orders per kind)."""
+    for n, permute in zip(R2R_LONG[kind], (True, False)):
         check_plan(P.PencilFFTPlan((n,), T.R2R(kind), real, extra_dims=(3,)), seed=n % 71)
-        for permute in (True, False):
-            check_plan(P.PencilFFTPlan((4, n), (T.FFT(), T.R2R(kind)), real, permute_dims=permute), seed=n % 67)
+        check_plan(P.PencilFFTPlan((4, n), (T.FFT(), T.R2R(kind)), real, permute_dims=permute), seed=n % 67)
 
 
 @pytest.mark.parametrize("real", [F64, F32])
