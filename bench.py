@@ -313,9 +313,12 @@ def _roofline(timing, steps):
             "kernel_share": d["ms"] / sum(v["ms"] for v in per.values())}
 
 
-def _timed(steps, warmup, step, plans=()):
+def _timed(steps, warmup, step, plans=(), stats=None):
     """ms per step (CUDA events on the current stream, synchronised on both
-    sides) and the plans' per-pass records of the timed steps."""
+    sides) and the plans' per-pass records of the timed steps; `stats`, when
+    given, receives the mean, std, min and max of the steps (one event
+    between consecutive steps)."""
+    import numpy as np
     import torch
     for _ in range(warmup):
         step()
@@ -323,18 +326,35 @@ def _timed(steps, warmup, step, plans=()):
     for p in plans:
         p.set_timing(True)
     stream = torch.cuda.current_stream()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps):
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    evs[0].record(stream)
+    for i in range(steps):
         step()
-    e1.record(stream)
+        evs[i + 1].record(stream)
     torch.cuda.synchronize()
     timing = []
     for p in plans:
         timing += p.get_timing()
         p.set_timing(False)
-    return e0.elapsed_time(e1) / steps, timing
+    if stats is not None:
+        per = np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(steps)])
+        stats.update(mean=float(per.mean()), std=float(per.std()), min=float(per.min()),
+                     max=float(per.max()), n=int(steps))
+    return evs[0].elapsed_time(evs[-1]) / steps, timing
+
+
+def _kernels(timing, steps):
+    """Per kernel of the timed steps: device ms per step, launches per step and
+    algorithmic GB/s (one read of each pass input + one write of its output)."""
+    per = {}
+    for e in timing:
+        k = per.setdefault(e["kernel"], {"ms": 0.0, "bytes": 0, "launches": 0})
+        k["ms"] += e["total_ms"]
+        k["bytes"] += e["bytes_per_launch"] * e["launches"]
+        k["launches"] += e["launches"]
+    return {name: {"ms_per_step": d["ms"] / steps, "launches_per_step": d["launches"] / steps,
+                   "gbs": d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] > 0 else None}
+            for name, d in sorted(per.items(), key=lambda kv: -kv[1]["ms"])}
 
 
 def _oracle_leg(forward, x, got):
@@ -358,7 +378,8 @@ def _round_trip_config(P, O, steps, warmup, dims, transforms, real, x, workload,
         P.mul_(v, plan, u)
         P.ldiv_(w, plan, v)
 
-    ms, timing = _timed(steps, warmup, step, (plan,))
+    stats = {}
+    ms, timing = _timed(steps, warmup, step, (plan,), stats)
     alg = sum(e["bytes_per_launch"] * e["launches"] for e in timing) / steps
     P.mul_(v, plan, u)
     P.ldiv_(w, plan, v)
@@ -369,11 +390,11 @@ def _round_trip_config(P, O, steps, warmup, dims, transforms, real, x, workload,
     with sfft.set_workers(threads):
         fwd_ms, err = _oracle_leg(orc.forward, x, got)
     out = {"workload": workload, "data": data, "dims": list(dims),
-           "value": ms, "unit": "ms", "metric": "round trip (mul! + ldiv!) ms",
+           "value": ms, "unit": "ms", "metric": "round trip (mul! + ldiv!) ms", "step_ms": stats,
            "forward_ms": sum(e["total_ms"] for e in timing if e["direction"] > 0) / steps,
            "backward_ms": sum(e["total_ms"] for e in timing if e["direction"] < 0) / steps,
            "alg_bytes_per_round_trip": alg, "hbm_gbs": alg / (ms * 1e-3) / 1e9,
-           "roofline": _roofline(timing, steps),
+           "roofline": _roofline(timing, steps), "kernels": _kernels(timing, steps),
            "rel_l2_forward_vs_oracle": err, "rel_l2_round_trip": _rel(back, x),
            "cpu_baseline": {"value": fwd_ms, "unit": "ms per forward", "cores": threads, "kind": "port",
                             "sample": "one forward transform of the same input (oracle, scipy.fft)"}}
