@@ -248,7 +248,10 @@ class PencilFFTPlan:
     extra_dims)`` mirrors the reference constructor ``src/plans.jl:306-320``;
     ``proc_dims`` must be all ones (one GPU, no MPI).  ``precision`` selects
     the kernel arithmetic: "default" (Float64 plans: double-float on the FP32
-    pipes for power-of-two lines, FP64 elsewhere), "native" (Float64 plans:
+    pipes for power-of-two, 3 * 2^k and 5 * 2^k lines, other lines up to 2048
+    points (Bluestein), the R2R kinds through their power-of-two forms or
+    extensions, and lines beyond one pass up to 2^23 points; FP64 for the
+    few lengths left, see the C header), "native" (Float64 plans:
     FP64 everywhere), "fx" (Float64 plans: block floating point, 64-bit
     integer components with one power-of-two scale per line, for
     power-of-two lines) or "tc" (Float32 plans: c2c lines of 256, 512 and
